@@ -1,0 +1,271 @@
+/*
+ * splat.h -- C ABI of libsplat, the GB300-native (sm_103a) forward trace step
+ * of SPLAT, the spectral photon-splatting ray tracer (xaellison/SPLAT).
+ *
+ * Every entry point returns a splat_status_t (SPLAT_OK == 0) and never
+ * throws; the message of the last failure on the calling thread is
+ * splat_last_error().  Device pointers are caller-owned and never freed by
+ * the library; the only library-owned objects are scenes (resident packed
+ * geometry + BVH).  Every call takes the caller's CUDA stream (cudaStream_t
+ * passed as void*; NULL is the legacy default stream) and enqueues
+ * asynchronously on it; nothing here synchronises the device except the
+ * *_host entry points, which wait for their own stream.
+ *
+ * Records keep the reference's Julia isbits layouts, so the Julia side can
+ * pass its own CuArray{ADRay}, CuArray{FTri}, CuArray{Tuple{Int32,Tri}}
+ * buffers (pointer(a)) without conversion.  Triangle indices are the
+ * reference's 1-based indices; a hit index of 1 means "miss" (index 1 is
+ * the all-zero sentinel triangle every scene starts with).
+ *
+ * Citations are path:line in the reference project.
+ */
+#ifndef SPLAT_H
+#define SPLAT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPLAT_ABI_VERSION 1
+
+typedef int32_t splat_status_t;
+enum {
+    SPLAT_OK = 0,
+    SPLAT_ERR_INVALID = 1,   /* bad argument (null pointer, size, enum) */
+    SPLAT_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+    SPLAT_ERR_ALLOC = 3,     /* a library-owned allocation failed */
+    SPLAT_ERR_WORKSPACE = 4, /* caller workspace smaller than required */
+    SPLAT_ERR_DEVICE = 5     /* a kernel reported an error status word */
+};
+
+/* ADRay, src/geo.jl:60-76 (136 bytes). status: 0 diffuse, 1 active, 2 infinity
+ * (src/geo.jl:78-80). */
+typedef struct splat_adray {
+    float pos[3];
+    float dp_dl[3];
+    float dp_dx[3];
+    float dp_dy[3];
+    float dir[3];
+    float dd_dl[3];
+    float dd_dx[3];
+    float dd_dy[3];
+    uint8_t in_medium;
+    uint8_t _pad0[7];
+    int64_t ignore_tri;
+    int64_t dest;
+    float lambda;
+    float x;
+    float y;
+    uint8_t status;
+    uint8_t _pad1[3];
+} splat_adray_t;
+
+/* FTri = SVector{10, R3}, src/geo.jl:18 (120 bytes): plane normal, v1, v2,
+ * v3, vertex normals n1..n3, texture coordinates (u, v, 0) of v1..v3. */
+typedef struct splat_ftri {
+    float v[10][3];
+} splat_ftri_t;
+
+/* Tuple{Int32, Tri}, the n_tris element of src/tracer.jl:313 (52 bytes):
+ * index, plane normal, v1, v2, v3. */
+typedef struct splat_ntri {
+    int32_t idx;
+    float v[4][3];
+} splat_ntri_t;
+
+/* RectLight, src/ray_generators.jl:4-11 (64 bytes). */
+typedef struct splat_rect_light {
+    float center[3];
+    float dir[3];
+    float dim1[3];
+    float dim2[3];
+    int64_t res1;
+    int64_t res2;
+} splat_rect_light_t;
+
+/* Glass index model.  LINEAR_REF is the reference's glass(lambda)
+ * (src/material.jl:1-9); CAUCHY n = a + b / lambda_um^2; SELLMEIER
+ * n^2 = 1 + sum_i sb[i] l2 / (l2 - sc[i]), l2 = lambda_um^2.  Air is 1. */
+enum { SPLAT_MATERIAL_LINEAR_REF = 0, SPLAT_MATERIAL_CAUCHY = 1, SPLAT_MATERIAL_SELLMEIER = 2 };
+typedef struct splat_material {
+    int32_t kind;
+    float a, b;
+    float sb[3];
+    float sc[3];
+} splat_material_t;
+
+/* Wavelength of generated rays: FIXED lambda0 (the reference hard-codes 550,
+ * src/ray_generators.jl:59), UNIFORM in [lambda0, lambda1), STRATIFIED: ray k
+ * uniform inside stratum (k mod n_strata). */
+enum { SPLAT_LAMBDA_FIXED = 0, SPLAT_LAMBDA_UNIFORM = 1, SPLAT_LAMBDA_STRATIFIED = 2 };
+typedef struct splat_lambda_mode {
+    int32_t mode;
+    int32_t n_strata;
+    float lambda0;
+    float lambda1;
+} splat_lambda_mode_t;
+
+enum { SPLAT_HITTER_BRUTE = 0, SPLAT_HITTER_BVH = 1 };
+enum { SPLAT_ACCUM_F32 = 0, SPLAT_ACCUM_I32 = 1 };
+
+/* flags */
+#define SPLAT_FLAG_REF_QUIRKS 1u /* reproduce the reference's derivative quirks (default) */
+
+typedef struct splat_scene splat_scene_t;
+
+typedef struct splat_scene_info {
+    int64_t n_tris;        /* including the sentinel */
+    int64_t first_diffuse; /* 1-based */
+    int64_t bvh_nodes;     /* 0 without BVH */
+    int64_t bvh_leaves;
+    int32_t bvh_depth;
+    int32_t bvh_max_leaf;
+    int64_t device_bytes;  /* library-owned device memory of this scene */
+    float bounds_lo[3];
+    float bounds_hi[3];
+    float bvh_pad;         /* absolute padding of the BVH boxes */
+} splat_scene_info_t;
+
+#define SPLAT_MAX_LAMBDA 64
+
+/* One forward trace step (the forward half of trace!, src/tracer.jl:317-342):
+ * rays_from_light -> depth x {next_hit!, rand!, evolve_ray} -> final_evolution
+ * -> atomic spectrum splat.  Rays ray_begin .. ray_end-1 of the light grid are
+ * traced (ray_end <= 0: the whole grid); ray ids are grid indices. */
+typedef struct splat_trace_params {
+    splat_rect_light_t light;
+    int64_t upscale;           /* forward_upscale: grid res / upscale rays, upscale^2 splat offsets */
+    splat_lambda_mode_t lambda_mode;
+    uint64_t seed;             /* Philox key: jitter, wavelength and Fresnel draws */
+    int32_t depth;
+    int32_t hitter;            /* SPLAT_HITTER_* */
+    splat_material_t material;
+    float force_rand;          /* < 0: draw; else every Fresnel draw is this value */
+    uint32_t flags;            /* SPLAT_FLAG_* */
+    int32_t n_lambda;          /* 0: each ray splats at its own wavelength into plane 0 */
+    float spectrum[SPLAT_MAX_LAMBDA];
+    int64_t map_w, map_h;      /* light map [w, h, planes], column-major (u fastest) */
+    int32_t accum;             /* SPLAT_ACCUM_* */
+    int32_t frac_bits;         /* fixed point: round(intensity * 2^frac_bits) */
+    int32_t zero_map;          /* 1: clear the map first; 0: accumulate onto it */
+    int32_t _pad;
+    int64_t ray_begin, ray_end;
+} splat_trace_params_t;
+
+/* Counters of one trace step, written on the device. */
+typedef struct splat_trace_stats {
+    int64_t rays_per_bounce[8]; /* active rays entering bounce b */
+    int64_t diffuse;            /* rays splatted */
+    int64_t samples;            /* splat samples accumulated (finite uv) */
+    int64_t error;              /* kernel error word, 0 = ok */
+    int64_t _pad;
+} splat_trace_stats_t;
+
+/* ---------------------------------------------------------------- library */
+int32_t splat_abi_version(void);
+const char* splat_last_error(void);
+/* Number of SMs and the device name of the current device (for reports). */
+splat_status_t splat_device_info(int32_t* sm_count, char* name, int32_t name_len);
+
+/* ------------------------------------------------------------------ scene */
+/* Resident scene: packed hit records, FTri optical data, optional BVH (host
+ * binned-SAH build, padded boxes).  Replaces the hitter constructors
+ * (src/alg_types.jl:60-90) and bv_partition / pack_bv_tris (src/bv.jl:68-136).
+ * host_tris: reference FTri array, index 1 the sentinel. */
+splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris, int64_t first_diffuse,
+                                  int32_t build_bvh, void* stream, splat_scene_t** out);
+splat_status_t splat_scene_destroy(splat_scene_t* scene);
+splat_status_t splat_scene_info(const splat_scene_t* scene, splat_scene_info_t* info);
+/* Device-side update from new FTri data of the same count (per-frame
+ * geometry upload): repacks the hit records and refits the BVH boxes
+ * bottom-up, keeping its topology.  d_tris: device FTri array. */
+splat_status_t splat_scene_update(splat_scene_t* scene, const splat_ftri_t* d_tris, void* stream);
+/* Device pointer of the scene's FTri array (read-only). */
+const splat_ftri_t* splat_scene_tris(const splat_scene_t* scene);
+
+/* -------------------------------------------------------- plugin boundary */
+/* rays_from_light (src/ray_generators.jl:64-97): (res1/upscale)*(res2/upscale)
+ * rays, column-major over (row, col), jitter from Philox(seed). */
+splat_status_t splat_rays_from_light(const splat_rect_light_t* light, int64_t upscale,
+                                     const splat_lambda_mode_t* lambda_mode, uint64_t seed, uint32_t light_index,
+                                     splat_adray_t* d_rays, void* stream);
+
+/* next_hit!(tracer, ::ExperimentalHitter6, rays, n_tris) (src/hitters.jl:205-226):
+ * brute-force nearest hit of every ray over the reference's n_tris array;
+ * lexicographic (t, index) minimum, packed into d_tmp (hitter.tmp, caller
+ * scratch of n_rays u64) then unpacked into d_hit_idx (tracer.hit_idx). */
+splat_status_t splat_next_hit_brute(const splat_adray_t* d_rays, int64_t n_rays, const splat_ntri_t* d_n_tris,
+                                    int64_t n_tris, uint64_t* d_tmp, int32_t* d_hit_idx, void* stream);
+
+/* next_hit! with a resident scene (brute force or BVH,
+ * src/hitters.jl:205-226 / 615-647).  d_hit_t (optional) receives the hit
+ * distance, Inf on a miss. */
+splat_status_t splat_next_hit(const splat_scene_t* scene, int32_t hitter, const splat_adray_t* d_rays,
+                              int64_t n_rays, int32_t* d_hit_idx, float* d_hit_t, void* stream);
+
+/* run_evolution! (src/tracer.jl:233-282) on the caller's rays, in place:
+ * depth x {hit, Fresnel draw, evolve_ray, compaction}, then the final hit of
+ * every ray into d_hit_idx.  Ray slot k draws Philox(seed, (k, 0, 1, bounce)).
+ * Workspace: splat_run_evolution_workspace_size(n_rays) bytes. */
+size_t splat_run_evolution_workspace_size(int64_t n_rays);
+splat_status_t splat_run_evolution(const splat_scene_t* scene, int32_t hitter, splat_adray_t* d_rays,
+                                   int64_t n_rays, int32_t depth, const splat_material_t* material,
+                                   float force_rand, uint64_t seed, uint32_t flags, int32_t* d_hit_idx,
+                                   void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* continuum_light_map2! (src/ray_imagers.jl:142-165): final_evolution of the
+ * diffuse rays (in place) and the atomic spectrum splat into d_tex
+ * ([w, h, planes] column-major, float or int32 fixed point).  spectrum is a
+ * host array of n_lambda wavelengths (n_lambda 0: own wavelength, 1 plane). */
+splat_status_t splat_continuum_light_map(const splat_scene_t* scene, splat_adray_t* d_rays, int64_t n_rays,
+                                         const int32_t* d_hit_idx, const float* spectrum, int32_t n_lambda,
+                                         int64_t upscale, void* d_tex, int32_t accum, int32_t frac_bits,
+                                         int64_t map_w, int64_t map_h, void* stream);
+
+/* ------------------------------------------------------- fused trace step */
+/* The GB300 form of the forward half of trace! (src/tracer.jl:317-342):
+ * structure-of-arrays ray state, compaction fused into evolve (ballot +
+ * block scan, one atomic per block, counts stay on the device), diffuse
+ * rays splatted inside the bounce that finds them, no host round trip.
+ * d_stats (optional) receives splat_trace_stats_t on the device. */
+size_t splat_trace_workspace_size(int64_t n_rays);
+splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace_params_t* params, void* d_map,
+                                   void* d_workspace, size_t workspace_bytes, splat_trace_stats_t* d_stats,
+                                   void* stream);
+/* Same step with host buffers: copies host_tris (n_tris FTri, the scene's
+ * triangle count) to the device, updates the scene (repack + BVH refit),
+ * traces, and copies the map back into host_map.  Pinned host memory is
+ * recommended.  Returns after the stream has finished. */
+splat_status_t splat_trace_forward_host(splat_scene_t* scene, const splat_ftri_t* host_tris,
+                                        const splat_trace_params_t* params, void* host_map, void* d_map,
+                                        void* d_workspace, size_t workspace_bytes, splat_trace_stats_t* host_stats,
+                                        void* stream);
+
+/* ------------------------------------------------------------- profiling */
+/* Launch profiling: while a profile is attached to the calling thread, every
+ * kernel libsplat launches from that thread is bracketed by CUDA events on
+ * the launch stream, per kernel kind.  splat_profile_read synchronises those
+ * events and returns the launch count and summed device time of one kind. */
+enum {
+    SPLAT_KERNEL_GENERATE = 0,
+    SPLAT_KERNEL_HIT_BRUTE = 1,
+    SPLAT_KERNEL_HIT_BVH = 2,
+    SPLAT_KERNEL_EVOLVE = 3,
+    SPLAT_KERNEL_AUX = 4, /* fills, unpacks, conversions, stats, refit, packing */
+    SPLAT_KERNEL_KINDS = 5
+};
+typedef struct splat_profile splat_profile_t;
+splat_status_t splat_profile_create(int32_t max_launches, splat_profile_t** out);
+splat_status_t splat_profile_attach(splat_profile_t* profile); /* NULL detaches */
+splat_status_t splat_profile_read(splat_profile_t* profile, int32_t kind, int64_t* launches, double* total_ms);
+splat_status_t splat_profile_reset(splat_profile_t* profile);
+splat_status_t splat_profile_destroy(splat_profile_t* profile);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPLAT_H */

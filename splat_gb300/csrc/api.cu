@@ -1,0 +1,682 @@
+// api.cu -- the extern "C" entry points of libsplat (include/splat.h).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "bvh_build.h"
+#include "kernels.h"
+
+using namespace splat;
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+namespace {
+
+thread_local std::string g_last_error;
+
+splat_status_t fail(splat_status_t code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+splat_status_t cuda_fail(cudaError_t e, const char* what) {
+    return fail(SPLAT_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define SPLAT_CUDA(call, what)                      \
+    do {                                            \
+        cudaError_t e_ = (call);                    \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+int sm_count_current() {
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+    if (dev >= 0 && dev < 64 && cache[dev]) return cache[dev];
+    int n = 152;
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (dev >= 0 && dev < 64) cache[dev] = n;
+    return n;
+}
+
+constexpr size_t kAlign = 256;
+size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+size_t soa_bytes(int64_t cap) {
+    return align_up((size_t)kPlanes * 4 * (size_t)cap) + 2 * align_up(4 * (size_t)cap) + align_up((size_t)cap);
+}
+
+RaySoA carve_soa(char*& p, int64_t cap) {
+    RaySoA s;
+    s.cap = cap;
+    s.f = reinterpret_cast<float*>(p);
+    p += align_up((size_t)kPlanes * 4 * (size_t)cap);
+    s.ignore = reinterpret_cast<int32_t*>(p);
+    p += align_up(4 * (size_t)cap);
+    s.id = reinterpret_cast<uint32_t*>(p);
+    p += align_up(4 * (size_t)cap);
+    s.medium = reinterpret_cast<uint8_t*>(p);
+    p += align_up((size_t)cap);
+    return s;
+}
+
+// Bounce-loop scratch: two SoA ray buffers, hit indices, the packed-argmin
+// array of split brute-force launches, counters and the kernel error word.
+struct Work {
+    RaySoA a, b;
+    int32_t* hit;
+    uint64_t* tmp;
+    int64_t* counts;  // counts[b] = active rays after bounce b (b <= 64)
+};
+constexpr size_t kCounterBytes = 1024;
+
+size_t work_bytes(int64_t cap) {
+    return 2 * soa_bytes(cap) + align_up(4 * (size_t)cap) + align_up(8 * (size_t)cap) + kCounterBytes + kAlign;
+}
+
+Work carve_work(void* ws, int64_t cap) {
+    char* p = reinterpret_cast<char*>(align_up(reinterpret_cast<size_t>(ws)));
+    Work w;
+    w.a = carve_soa(p, cap);
+    w.b = carve_soa(p, cap);
+    w.hit = reinterpret_cast<int32_t*>(p);
+    p += align_up(4 * (size_t)cap);
+    w.tmp = reinterpret_cast<uint64_t*>(p);
+    p += align_up(8 * (size_t)cap);
+    w.counts = reinterpret_cast<int64_t*>(p);
+    return w;
+}
+
+bool valid_material(const splat_material_t* m) {
+    return m && m->kind >= SPLAT_MATERIAL_LINEAR_REF && m->kind <= SPLAT_MATERIAL_SELLMEIER;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// launch profiling
+// ---------------------------------------------------------------------------
+struct splat_profile {
+    int32_t max = 0;
+    int32_t used = 0;
+    std::vector<cudaEvent_t> ev;  // 2 per scope
+    std::vector<int32_t> kind;
+    std::vector<int64_t> kernels;  // kernels launched inside the scope
+};
+
+namespace {
+thread_local splat_profile* g_prof = nullptr;
+
+// Brackets one launcher call with events on its stream while a profile is
+// attached to this thread.
+struct ProfScope {
+    int idx = -1;
+    cudaStream_t s;
+    int64_t k0;
+    ProfScope(int kind, cudaStream_t st) : s(st), k0(g_launches) {
+        splat_profile* p = g_prof;
+        if (p && p->used < p->max) {
+            idx = p->used++;
+            p->kind[(size_t)idx] = kind;
+            cudaEventRecord(p->ev[2 * (size_t)idx], s);
+        }
+    }
+    ~ProfScope() {
+        if (idx >= 0 && g_prof) {
+            g_prof->kernels[(size_t)idx] = g_launches - k0;
+            cudaEventRecord(g_prof->ev[2 * (size_t)idx + 1], s);
+        }
+    }
+};
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// scene
+// ---------------------------------------------------------------------------
+struct splat_scene {
+    int device = 0;
+    int64_t n_tris = 0, first_diffuse = 0;
+    splat_ftri_t* d_ftri = nullptr;
+    TriHit* d_brute = nullptr;
+    int64_t n_recs = 0;
+    BvhNode* d_nodes = nullptr;
+    int64_t n_nodes = 0;
+    TriHit* d_bvh = nullptr;
+    int32_t* d_order = nullptr;
+    int32_t* d_levels = nullptr;
+    std::vector<int64_t> level_off;
+    int depth = 0, max_leaf = 0;
+    int64_t leaves = 0;
+    float pad_abs = 0.f, pad_rel = 0.f;
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    int32_t* d_err = nullptr;
+    int64_t bytes = 0;
+};
+
+static void scene_free(splat_scene* s) {
+    if (!s) return;
+    cudaFree(s->d_ftri);
+    cudaFree(s->d_brute);
+    cudaFree(s->d_nodes);
+    cudaFree(s->d_bvh);
+    cudaFree(s->d_order);
+    cudaFree(s->d_levels);
+    cudaFree(s->d_err);
+    delete s;
+}
+
+template <class T>
+static cudaError_t dalloc(T** p, size_t bytes, int64_t& total) {
+    total += (int64_t)bytes;
+    return cudaMalloc(reinterpret_cast<void**>(p), bytes < 16 ? 16 : bytes);
+}
+
+static splat_status_t scene_pack(splat_scene* s, cudaStream_t st) {
+    ProfScope ps(SPLAT_KERNEL_AUX, st);
+    cudaError_t e = launch_pack_hits(s->d_ftri, s->n_tris, s->d_brute, s->d_order, s->d_bvh, st);
+    if (e != cudaSuccess) return cuda_fail(e, "pack hit records");
+    if (s->d_nodes) {
+        for (size_t l = 0; l + 1 < s->level_off.size(); ++l) {
+            const int64_t a = s->level_off[l], b = s->level_off[l + 1];
+            e = launch_refit_level(s->d_nodes, s->d_levels + a, b - a, s->d_bvh, s->d_ftri, s->pad_abs, s->pad_rel, st);
+            if (e != cudaSuccess) return cuda_fail(e, "BVH refit");
+        }
+    }
+    return SPLAT_OK;
+}
+
+extern "C" {
+
+int32_t splat_abi_version(void) { return SPLAT_ABI_VERSION; }
+
+const char* splat_last_error(void) { return g_last_error.c_str(); }
+
+splat_status_t splat_device_info(int32_t* sm_count, char* name, int32_t name_len) {
+    int dev = 0;
+    SPLAT_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    cudaDeviceProp prop;
+    SPLAT_CUDA(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
+    if (sm_count) *sm_count = prop.multiProcessorCount;
+    if (name && name_len > 0) {
+        std::strncpy(name, prop.name, (size_t)name_len - 1);
+        name[name_len - 1] = 0;
+    }
+    return SPLAT_OK;
+}
+
+splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris, int64_t first_diffuse,
+                                  int32_t build_bvh_flag, void* stream, splat_scene_t** out) {
+    if (!out) return fail(SPLAT_ERR_INVALID, "scene_create: out is null");
+    *out = nullptr;
+    if (!host_tris || n_tris < 1) return fail(SPLAT_ERR_INVALID, "scene_create: need at least the sentinel triangle");
+    if (n_tris >= (int64_t(1) << 31)) return fail(SPLAT_ERR_INVALID, "scene_create: too many triangles");
+    if (first_diffuse < 1) return fail(SPLAT_ERR_INVALID, "scene_create: first_diffuse must be >= 1");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    splat_scene* s = new (std::nothrow) splat_scene();
+    if (!s) return fail(SPLAT_ERR_ALLOC, "scene_create: host allocation");
+    cudaGetDevice(&s->device);
+    s->n_tris = n_tris;
+    s->first_diffuse = first_diffuse;
+    s->n_recs = n_tris - 1;
+    for (int a = 0; a < 3; ++a) {
+        s->lo[a] = INFINITY;
+        s->hi[a] = -INFINITY;
+    }
+    for (int64_t j = 1; j < n_tris; ++j)
+        for (int v = 1; v < 4; ++v)
+            for (int a = 0; a < 3; ++a) {
+                s->lo[a] = std::min(s->lo[a], host_tris[j].v[v][a]);
+                s->hi[a] = std::max(s->hi[a], host_tris[j].v[v][a]);
+            }
+    BvhHost bvh;
+    if (build_bvh_flag) {
+        std::string err;
+        if (!build_bvh(host_tris, n_tris, bvh, err)) {
+            delete s;
+            return fail(SPLAT_ERR_INVALID, "scene_create: " + err);
+        }
+    }
+    cudaError_t e = cudaSuccess;
+    auto chk = [&](cudaError_t x) {
+        if (e == cudaSuccess && x != cudaSuccess) e = x;
+    };
+    chk(dalloc(&s->d_ftri, sizeof(splat_ftri_t) * (size_t)n_tris, s->bytes));
+    chk(dalloc(&s->d_brute, sizeof(TriHit) * (size_t)s->n_recs, s->bytes));
+    chk(dalloc(&s->d_err, sizeof(int32_t) * 4, s->bytes));
+    if (build_bvh_flag && !bvh.nodes.empty()) {
+        s->n_nodes = (int64_t)bvh.nodes.size();
+        chk(dalloc(&s->d_nodes, sizeof(BvhNode) * bvh.nodes.size(), s->bytes));
+        chk(dalloc(&s->d_bvh, sizeof(TriHit) * (size_t)s->n_recs, s->bytes));
+        chk(dalloc(&s->d_order, sizeof(int32_t) * bvh.order.size(), s->bytes));
+        chk(dalloc(&s->d_levels, sizeof(int32_t) * bvh.level_nodes.size(), s->bytes));
+        s->level_off = bvh.level_off;
+        s->depth = bvh.depth;
+        s->max_leaf = bvh.max_leaf;
+        s->leaves = bvh.leaves;
+        s->pad_abs = bvh.pad_abs;
+        s->pad_rel = bvh.pad_rel;
+    }
+    if (e != cudaSuccess) {
+        scene_free(s);
+        return fail(SPLAT_ERR_ALLOC, std::string("scene_create: cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    chk(cudaMemcpyAsync(s->d_ftri, host_tris, sizeof(splat_ftri_t) * (size_t)n_tris, cudaMemcpyHostToDevice, st));
+    chk(cudaMemsetAsync(s->d_err, 0, sizeof(int32_t) * 4, st));
+    if (s->d_nodes) {
+        chk(cudaMemcpyAsync(s->d_nodes, bvh.nodes.data(), sizeof(BvhNode) * bvh.nodes.size(), cudaMemcpyHostToDevice,
+                            st));
+        chk(cudaMemcpyAsync(s->d_order, bvh.order.data(), sizeof(int32_t) * bvh.order.size(), cudaMemcpyHostToDevice,
+                            st));
+        chk(cudaMemcpyAsync(s->d_levels, bvh.level_nodes.data(), sizeof(int32_t) * bvh.level_nodes.size(),
+                            cudaMemcpyHostToDevice, st));
+    }
+    if (e == cudaSuccess) chk(launch_pack_hits(s->d_ftri, n_tris, s->d_brute, s->d_order, s->d_bvh, st));
+    // host vectors above must outlive the async copies
+    if (e == cudaSuccess) chk(cudaStreamSynchronize(st));
+    if (e != cudaSuccess) {
+        scene_free(s);
+        return cuda_fail(e, "scene_create");
+    }
+    *out = s;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_scene_destroy(splat_scene_t* scene) {
+    if (!scene) return fail(SPLAT_ERR_INVALID, "scene_destroy: null scene");
+    scene_free(scene);
+    return SPLAT_OK;
+}
+
+splat_status_t splat_scene_info(const splat_scene_t* s, splat_scene_info_t* info) {
+    if (!s || !info) return fail(SPLAT_ERR_INVALID, "scene_info: null argument");
+    std::memset(info, 0, sizeof(*info));
+    info->n_tris = s->n_tris;
+    info->first_diffuse = s->first_diffuse;
+    info->bvh_nodes = s->n_nodes;
+    info->bvh_leaves = s->leaves;
+    info->bvh_depth = s->depth;
+    info->bvh_max_leaf = s->max_leaf;
+    info->device_bytes = s->bytes;
+    for (int a = 0; a < 3; ++a) {
+        info->bounds_lo[a] = s->lo[a];
+        info->bounds_hi[a] = s->hi[a];
+    }
+    info->bvh_pad = s->pad_abs;
+    return SPLAT_OK;
+}
+
+const splat_ftri_t* splat_scene_tris(const splat_scene_t* s) { return s ? s->d_ftri : nullptr; }
+
+splat_status_t splat_scene_update(splat_scene_t* s, const splat_ftri_t* d_tris, void* stream) {
+    if (!s || !d_tris) return fail(SPLAT_ERR_INVALID, "scene_update: null argument");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (d_tris != s->d_ftri)
+        SPLAT_CUDA(cudaMemcpyAsync(s->d_ftri, d_tris, sizeof(splat_ftri_t) * (size_t)s->n_tris,
+                                   cudaMemcpyDeviceToDevice, st),
+                   "scene_update copy");
+    return scene_pack(s, st);
+}
+
+// ---------------------------------------------------------------------------
+// plugin boundary
+// ---------------------------------------------------------------------------
+static bool light_ok(const splat_rect_light_t* L, int64_t upscale) {
+    return L && upscale >= 1 && L->res1 / upscale >= 1 && L->res2 / upscale >= 1;
+}
+
+splat_status_t splat_rays_from_light(const splat_rect_light_t* light, int64_t upscale,
+                                     const splat_lambda_mode_t* lambda_mode, uint64_t seed, uint32_t light_index,
+                                     splat_adray_t* d_rays, void* stream) {
+    if (!light_ok(light, upscale) || !d_rays) return fail(SPLAT_ERR_INVALID, "rays_from_light: bad light or output");
+    GenParams g;
+    g.light = *light;
+    g.upscale = upscale;
+    g.lm = lambda_mode ? *lambda_mode : splat_lambda_mode_t{SPLAT_LAMBDA_FIXED, 1, 550.0f, 550.0f};
+    if (g.lm.mode == SPLAT_LAMBDA_STRATIFIED && g.lm.n_strata < 1) return fail(SPLAT_ERR_INVALID, "n_strata < 1");
+    g.seed = seed;
+    g.light_index = light_index;
+    g.ray_begin = 0;
+    const int64_t n = (light->res1 / upscale) * (light->res2 / upscale);
+    ProfScope ps(SPLAT_KERNEL_GENERATE, reinterpret_cast<cudaStream_t>(stream));
+    SPLAT_CUDA(launch_generate_aos(g, n, d_rays, reinterpret_cast<cudaStream_t>(stream)), "rays_from_light");
+    return SPLAT_OK;
+}
+
+splat_status_t splat_next_hit_brute(const splat_adray_t* d_rays, int64_t n_rays, const splat_ntri_t* d_n_tris,
+                                    int64_t n_tris, uint64_t* d_tmp, int32_t* d_hit_idx, void* stream) {
+    if (n_rays < 0 || n_tris < 0) return fail(SPLAT_ERR_INVALID, "next_hit_brute: negative size");
+    if (n_rays == 0) return SPLAT_OK;
+    if (!d_rays || !d_tmp || !d_hit_idx || (n_tris > 0 && !d_n_tris))
+        return fail(SPLAT_ERR_INVALID, "next_hit_brute: null pointer");
+    ProfScope ps(SPLAT_KERNEL_HIT_BRUTE, reinterpret_cast<cudaStream_t>(stream));
+    SPLAT_CUDA(launch_hit_brute_ntris(d_rays, n_rays, d_n_tris, n_tris, d_tmp, d_hit_idx, sm_count_current(),
+                                      reinterpret_cast<cudaStream_t>(stream)),
+               "next_hit_brute");
+    return SPLAT_OK;
+}
+
+static splat_status_t hit_any(const splat_scene_t* s, int32_t hitter, const RaySrc& src, int64_t cap,
+                              int32_t* hit_idx, float* hit_t, uint64_t* tmp, cudaStream_t st) {
+    cudaError_t e;
+    ProfScope ps(hitter == SPLAT_HITTER_BVH && s->d_nodes ? SPLAT_KERNEL_HIT_BVH : SPLAT_KERNEL_HIT_BRUTE, st);
+    if (hitter == SPLAT_HITTER_BVH) {
+        if (!s->d_nodes) {
+            if (s->n_recs > 0) return fail(SPLAT_ERR_INVALID, "BVH hitter on a scene created without BVH");
+            e = launch_hit_brute(src, cap, s->d_brute, 0, hit_idx, hit_t, nullptr, s->d_err, sm_count_current(), st);
+        } else {
+            e = launch_hit_bvh(src, cap, BvhView{s->d_nodes, s->d_bvh}, hit_idx, hit_t, s->d_err, sm_count_current(),
+                               st);
+        }
+    } else if (hitter == SPLAT_HITTER_BRUTE) {
+        e = launch_hit_brute(src, cap, s->d_brute, s->n_recs, hit_idx, hit_t, tmp, s->d_err, sm_count_current(), st);
+    } else {
+        return fail(SPLAT_ERR_INVALID, "unknown hitter");
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "hit kernel");
+    return SPLAT_OK;
+}
+
+splat_status_t splat_next_hit(const splat_scene_t* scene, int32_t hitter, const splat_adray_t* d_rays, int64_t n_rays,
+                              int32_t* d_hit_idx, float* d_hit_t, void* stream) {
+    if (!scene || n_rays < 0) return fail(SPLAT_ERR_INVALID, "next_hit: bad scene or size");
+    if (n_rays == 0) return SPLAT_OK;
+    if (!d_rays || !d_hit_idx) return fail(SPLAT_ERR_INVALID, "next_hit: null pointer");
+    RaySrc src{};
+    src.aos = d_rays;
+    src.n = n_rays;
+    return hit_any(scene, hitter, src, n_rays, d_hit_idx, d_hit_t, nullptr, reinterpret_cast<cudaStream_t>(stream));
+}
+
+size_t splat_run_evolution_workspace_size(int64_t n_rays) { return n_rays <= 0 ? kAlign : work_bytes(n_rays); }
+
+static SplatParams make_splat(const float* spectrum, int32_t n_lambda, int64_t upscale, void* map, int32_t accum,
+                              int32_t frac_bits, int64_t w, int64_t h) {
+    SplatParams sp;
+    std::memset(&sp, 0, sizeof(sp));
+    sp.map = map;
+    sp.accum = accum;
+    sp.scale = std::ldexp(1.0f, frac_bits);
+    sp.w = w;
+    sp.h = h;
+    sp.n_lambda = n_lambda;
+    for (int i = 0; i < n_lambda; ++i) sp.spectrum[i] = spectrum[i];
+    sp.n_delta = (int32_t)upscale;
+    // upres(N), src/alg_types.jl:108
+    for (int k = 1; k <= sp.n_delta; ++k)
+        sp.deltas[k - 1] = ((float)k / (float)sp.n_delta - 0.5f) - (1.0f / (2.0f * (float)sp.n_delta));
+    return sp;
+}
+
+static splat_status_t check_map(const float* spectrum, int32_t n_lambda, int64_t upscale, const void* map,
+                                int32_t accum, int32_t frac_bits, int64_t w, int64_t h) {
+    if (!map) return fail(SPLAT_ERR_INVALID, "light map is null");
+    if (n_lambda < 0 || n_lambda > SPLAT_MAX_LAMBDA || (n_lambda > 0 && !spectrum))
+        return fail(SPLAT_ERR_INVALID, "n_lambda must be 0..64 with a spectrum");
+    if (upscale < 1 || upscale > 16) return fail(SPLAT_ERR_INVALID, "upscale must be 1..16");
+    if (accum != SPLAT_ACCUM_F32 && accum != SPLAT_ACCUM_I32) return fail(SPLAT_ERR_INVALID, "unknown accumulation");
+    if (frac_bits < 0 || frac_bits > 30) return fail(SPLAT_ERR_INVALID, "frac_bits must be 0..30");
+    if (w < 1 || h < 1 || w > (1 << 24) || h > (1 << 24)) return fail(SPLAT_ERR_INVALID, "bad light map size");
+    return SPLAT_OK;
+}
+
+splat_status_t splat_run_evolution(const splat_scene_t* scene, int32_t hitter, splat_adray_t* d_rays, int64_t n_rays,
+                                   int32_t depth, const splat_material_t* material, float force_rand, uint64_t seed,
+                                   uint32_t flags, int32_t* d_hit_idx, void* d_workspace, size_t workspace_bytes,
+                                   void* stream) {
+    if (!scene || n_rays < 0 || depth < 0 || depth > 64) return fail(SPLAT_ERR_INVALID, "run_evolution: bad arguments");
+    if (!valid_material(material)) return fail(SPLAT_ERR_INVALID, "run_evolution: bad material");
+    if (n_rays == 0) return SPLAT_OK;
+    if (!d_rays || !d_hit_idx || !d_workspace) return fail(SPLAT_ERR_INVALID, "run_evolution: null pointer");
+    if (workspace_bytes < work_bytes(n_rays)) return fail(SPLAT_ERR_WORKSPACE, "run_evolution: workspace too small");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    Work w = carve_work(d_workspace, n_rays);
+    SPLAT_CUDA(cudaMemsetAsync(w.counts, 0, kCounterBytes, st), "memset counters");
+    {
+        ProfScope ps(SPLAT_KERNEL_AUX, st);
+        SPLAT_CUDA(launch_aos_to_soa(d_rays, n_rays, w.a, &w.counts[0], st), "aos_to_soa");
+    }
+    RaySoA cur = w.a, nxt = w.b;
+    EvolveArgs ea;
+    std::memset(&ea, 0, sizeof(ea));
+    ea.tris = scene->d_ftri;
+    ea.n_tris = scene->n_tris;
+    ea.err = scene->d_err;
+    ea.first_diffuse = scene->first_diffuse;
+    ea.material = *material;
+    ea.seed = seed;
+    ea.force_rand = force_rand;
+    ea.quirks = (flags & SPLAT_FLAG_REF_QUIRKS) ? 1 : 0;
+    ea.aos = d_rays;
+    for (int32_t b = 1; b <= depth; ++b) {
+        RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0};
+        splat_status_t rc = hit_any(scene, hitter, src, n_rays, w.hit, nullptr, w.tmp, st);
+        if (rc != SPLAT_OK) return rc;
+        ea.in = cur;
+        ea.out = nxt;
+        ea.in_count = &w.counts[b - 1];
+        ea.out_count = &w.counts[b];
+        ea.hit_idx = w.hit;
+        ea.bounce = (uint32_t)b;
+        ea.last = 0;
+        {
+            ProfScope ps(SPLAT_KERNEL_EVOLVE, st);
+            SPLAT_CUDA(launch_evolve_plugin(ea, n_rays, sm_count_current(), st), "evolve");
+        }
+        std::swap(cur, nxt);
+    }
+    {
+        ProfScope ps(SPLAT_KERNEL_AUX, st);
+        SPLAT_CUDA(launch_soa_to_aos(cur, &w.counts[depth], d_rays, kStatusActive, st), "soa_to_aos");
+    }
+    // realign: the hit of every ray's final state (src/tracer.jl:279-280)
+    RaySrc all{};
+    all.aos = d_rays;
+    all.n = n_rays;
+    return hit_any(scene, hitter, all, n_rays, d_hit_idx, nullptr, w.tmp, st);
+}
+
+splat_status_t splat_continuum_light_map(const splat_scene_t* scene, splat_adray_t* d_rays, int64_t n_rays,
+                                         const int32_t* d_hit_idx, const float* spectrum, int32_t n_lambda,
+                                         int64_t upscale, void* d_tex, int32_t accum, int32_t frac_bits,
+                                         int64_t map_w, int64_t map_h, void* stream) {
+    if (!scene || n_rays < 0) return fail(SPLAT_ERR_INVALID, "continuum_light_map: bad arguments");
+    splat_status_t rc = check_map(spectrum, n_lambda, upscale, d_tex, accum, frac_bits, map_w, map_h);
+    if (rc != SPLAT_OK) return rc;
+    if (n_rays == 0) return SPLAT_OK;
+    if (!d_rays || !d_hit_idx) return fail(SPLAT_ERR_INVALID, "continuum_light_map: null pointer");
+    SplatParams sp = make_splat(spectrum, n_lambda, upscale, d_tex, accum, frac_bits, map_w, map_h);
+    ProfScope ps(SPLAT_KERNEL_EVOLVE, reinterpret_cast<cudaStream_t>(stream));
+    SPLAT_CUDA(launch_light_map(d_rays, n_rays, d_hit_idx, scene->d_ftri, scene->n_tris, scene->d_err, sp,
+                                sm_count_current(),
+                                reinterpret_cast<cudaStream_t>(stream)),
+               "light map");
+    return SPLAT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// fused trace step
+// ---------------------------------------------------------------------------
+size_t splat_trace_workspace_size(int64_t n_rays) { return n_rays <= 0 ? kAlign : work_bytes(n_rays); }
+
+static int64_t grid_rays(const splat_trace_params_t* P) {
+    return (P->light.res1 / P->upscale) * (P->light.res2 / P->upscale);
+}
+
+splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace_params_t* P, void* d_map,
+                                   void* d_workspace, size_t workspace_bytes, splat_trace_stats_t* d_stats,
+                                   void* stream) {
+    if (!scene || !P) return fail(SPLAT_ERR_INVALID, "trace_forward: null scene or params");
+    if (!light_ok(&P->light, P->upscale)) return fail(SPLAT_ERR_INVALID, "trace_forward: bad light / upscale");
+    if (P->depth < 1 || P->depth > 8) return fail(SPLAT_ERR_INVALID, "trace_forward: depth must be 1..8");
+    if (!valid_material(&P->material)) return fail(SPLAT_ERR_INVALID, "trace_forward: bad material");
+    if (P->lambda_mode.mode == SPLAT_LAMBDA_STRATIFIED && P->lambda_mode.n_strata < 1)
+        return fail(SPLAT_ERR_INVALID, "trace_forward: n_strata < 1");
+    splat_status_t rc =
+        check_map(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
+    if (rc != SPLAT_OK) return rc;
+    if (P->hitter == SPLAT_HITTER_BVH && !scene->d_nodes && scene->n_recs > 0)
+        return fail(SPLAT_ERR_INVALID, "trace_forward: BVH hitter on a scene without BVH");
+    const int64_t n_grid = grid_rays(P);
+    const int64_t rb = P->ray_begin < 0 ? 0 : P->ray_begin;
+    const int64_t re = (P->ray_end <= 0 || P->ray_end > n_grid) ? n_grid : P->ray_end;
+    if (n_grid >= (int64_t(1) << 32)) return fail(SPLAT_ERR_INVALID, "trace_forward: more than 2^32 rays");
+    const int64_t cnt = re - rb;
+    if (cnt <= 0) return fail(SPLAT_ERR_INVALID, "trace_forward: empty ray range");
+    if (!d_workspace || workspace_bytes < work_bytes(cnt))
+        return fail(SPLAT_ERR_WORKSPACE, "trace_forward: workspace smaller than splat_trace_workspace_size");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int sm = sm_count_current();
+    Work w = carve_work(d_workspace, cnt);
+    SPLAT_CUDA(cudaMemsetAsync(w.counts, 0, kCounterBytes, st), "memset counters");
+    if (d_stats) SPLAT_CUDA(cudaMemsetAsync(d_stats, 0, sizeof(splat_trace_stats_t), st), "memset stats");
+    const int64_t planes = P->n_lambda > 0 ? P->n_lambda : 1;
+    if (P->zero_map) SPLAT_CUDA(cudaMemsetAsync(d_map, 0, (size_t)P->map_w * P->map_h * planes * 4, st), "clear map");
+
+    GenParams g;
+    g.light = P->light;
+    g.upscale = P->upscale;
+    g.lm = P->lambda_mode;
+    g.seed = P->seed;
+    g.light_index = 0;
+    g.ray_begin = rb;
+    {
+        ProfScope ps(SPLAT_KERNEL_GENERATE, st);
+        SPLAT_CUDA(launch_generate_soa(g, cnt, w.a, &w.counts[0], st), "generate");
+    }
+
+    EvolveArgs ea;
+    std::memset(&ea, 0, sizeof(ea));
+    ea.tris = scene->d_ftri;
+    ea.n_tris = scene->n_tris;
+    ea.err = scene->d_err;
+    ea.first_diffuse = scene->first_diffuse;
+    ea.material = P->material;
+    ea.seed = P->seed;
+    ea.force_rand = P->force_rand;
+    ea.quirks = (P->flags & SPLAT_FLAG_REF_QUIRKS) ? 1 : 0;
+    ea.sp = make_splat(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
+    ea.stats = d_stats;
+    RaySoA cur = w.a, nxt = w.b;
+    for (int32_t b = 1; b <= P->depth; ++b) {
+        RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0};
+        rc = hit_any(scene, P->hitter, src, cnt, w.hit, nullptr, w.tmp, st);
+        if (rc != SPLAT_OK) return rc;
+        ea.in = cur;
+        ea.out = nxt;
+        ea.in_count = &w.counts[b - 1];
+        ea.out_count = &w.counts[b];
+        ea.hit_idx = w.hit;
+        ea.bounce = (uint32_t)b;
+        ea.last = b == P->depth ? 1 : 0;
+        {
+            ProfScope ps(SPLAT_KERNEL_EVOLVE, st);
+            SPLAT_CUDA(launch_evolve_trace(ea, cnt, sm, st), "evolve");
+        }
+        std::swap(cur, nxt);
+    }
+    if (d_stats) {
+        ProfScope ps(SPLAT_KERNEL_AUX, st);
+        SPLAT_CUDA(launch_stats_finish(w.counts, P->depth, d_stats, scene->d_err, st), "stats");
+    }
+    return SPLAT_OK;
+}
+
+splat_status_t splat_trace_forward_host(splat_scene_t* scene, const splat_ftri_t* host_tris,
+                                        const splat_trace_params_t* P, void* host_map, void* d_map, void* d_workspace,
+                                        size_t workspace_bytes, splat_trace_stats_t* host_stats, void* stream) {
+    if (!scene || !P || !host_map) return fail(SPLAT_ERR_INVALID, "trace_forward_host: null argument");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (host_tris) {
+        SPLAT_CUDA(cudaMemcpyAsync(scene->d_ftri, host_tris, sizeof(splat_ftri_t) * (size_t)scene->n_tris,
+                                   cudaMemcpyHostToDevice, st),
+                   "upload triangles");
+        splat_status_t rc = scene_pack(scene, st);
+        if (rc != SPLAT_OK) return rc;
+    }
+    // stats live at the end of the workspace's counter block
+    splat_status_t rc = splat_trace_forward(scene, P, d_map, d_workspace, workspace_bytes, nullptr, stream);
+    if (rc != SPLAT_OK) return rc;
+    const int64_t planes = P->n_lambda > 0 ? P->n_lambda : 1;
+    SPLAT_CUDA(cudaMemcpyAsync(host_map, d_map, (size_t)P->map_w * P->map_h * planes * 4, cudaMemcpyDeviceToHost, st),
+               "download map");
+    if (host_stats) {
+        std::memset(host_stats, 0, sizeof(*host_stats));
+        const int64_t n_grid = grid_rays(P);
+        const int64_t rb = P->ray_begin < 0 ? 0 : P->ray_begin;
+        const int64_t re = (P->ray_end <= 0 || P->ray_end > n_grid) ? n_grid : P->ray_end;
+        Work w = carve_work(d_workspace, re - rb);
+        SPLAT_CUDA(cudaMemcpyAsync(host_stats->rays_per_bounce, w.counts, sizeof(int64_t) * (size_t)P->depth,
+                                   cudaMemcpyDeviceToHost, st),
+                   "download counters");
+    }
+    SPLAT_CUDA(cudaStreamSynchronize(st), "trace_forward_host sync");
+    int32_t err = 0;
+    SPLAT_CUDA(cudaMemcpy(&err, scene->d_err, sizeof(err), cudaMemcpyDeviceToHost), "read error word");
+    if (err) return fail(SPLAT_ERR_DEVICE, "trace_forward_host: kernel error word " + std::to_string(err));
+    return SPLAT_OK;
+}
+
+splat_status_t splat_profile_create(int32_t max_launches, splat_profile_t** out) {
+    if (!out || max_launches < 1 || max_launches > (1 << 20)) return fail(SPLAT_ERR_INVALID, "profile_create: bad argument");
+    splat_profile* p = new (std::nothrow) splat_profile();
+    if (!p) return fail(SPLAT_ERR_ALLOC, "profile_create: host allocation");
+    p->max = max_launches;
+    p->ev.resize(2 * (size_t)max_launches);
+    p->kind.assign((size_t)max_launches, 0);
+    p->kernels.assign((size_t)max_launches, 0);
+    for (auto& e : p->ev) {
+        cudaError_t r = cudaEventCreate(&e);
+        if (r != cudaSuccess) {
+            for (auto& x : p->ev)
+                if (x) cudaEventDestroy(x);
+            delete p;
+            return cuda_fail(r, "profile_create: cudaEventCreate");
+        }
+    }
+    *out = p;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_profile_attach(splat_profile_t* profile) {
+    g_prof = profile;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_profile_reset(splat_profile_t* p) {
+    if (!p) return fail(SPLAT_ERR_INVALID, "profile_reset: null profile");
+    p->used = 0;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_profile_read(splat_profile_t* p, int32_t kind, int64_t* launches, double* total_ms) {
+    if (!p || kind < 0 || kind > SPLAT_KERNEL_KINDS) return fail(SPLAT_ERR_INVALID, "profile_read: bad argument");
+    int64_t n = 0;
+    double ms = 0.0;
+    for (int32_t i = 0; i < p->used; ++i) {
+        if (kind != SPLAT_KERNEL_KINDS && p->kind[(size_t)i] != kind) continue;
+        SPLAT_CUDA(cudaEventSynchronize(p->ev[2 * (size_t)i + 1]), "profile_read: sync");
+        float t = 0.f;
+        SPLAT_CUDA(cudaEventElapsedTime(&t, p->ev[2 * (size_t)i], p->ev[2 * (size_t)i + 1]), "profile_read: elapsed");
+        ms += t;
+        n += p->kernels[(size_t)i];
+    }
+    if (launches) *launches = n;
+    if (total_ms) *total_ms = ms;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_profile_destroy(splat_profile_t* p) {
+    if (!p) return fail(SPLAT_ERR_INVALID, "profile_destroy: null profile");
+    if (g_prof == p) g_prof = nullptr;
+    for (auto& e : p->ev) cudaEventDestroy(e);
+    delete p;
+    return SPLAT_OK;
+}
+
+}  // extern "C"

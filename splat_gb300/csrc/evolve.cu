@@ -1,0 +1,386 @@
+// evolve.cu -- evolve_ray over the active rays of one bounce, with the ray
+// compaction (warp ballot + block scan, one atomic per block) fused in, and
+// in trace mode the diffuse rays' final_evolution + light-map splat fused in
+// as well, so a diffuse ray is splatted in the bounce that finds it and never
+// stored.
+//
+// Reference: evolve_ray src/tracer.jl:181-201, partition! src/partition.jl
+// (semantics: the active rays, in any order, and their count),
+// final_evolution src/ray_imagers.jl:4-37, atomic_spectrum_kernel2
+// src/ray_imagers.jl:78-113.  Each ray's Fresnel draw is keyed by its id, so
+// results do not depend on the order compaction leaves the rays in.
+//
+// Splat: a warp takes its diffuse rays one at a time (state broadcast by
+// shuffles) and spreads that ray's n_lambda x N x N samples over its lanes.
+// Fixed-point maps add round(intensity * 2^frac_bits) with warp-aggregated
+// integer atomics (lanes on the same texel are summed by match_any +
+// reduce_add first), which makes the map independent of ray order and
+// bit-exact run to run.  Float maps use plain float atomics, as the
+// reference does.
+#include "kernels.h"
+#include "optics.cuh"
+
+namespace splat {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kEvolveThreads = 256;
+
+__device__ __forceinline__ F3 shfl3(F3 v, int src) {
+    return {__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src), __shfl_sync(kFull, v.z, src)};
+}
+
+__device__ __forceinline__ RayState shfl_ray(const RayState& r, int src) {
+    RayState q;
+    q.pos = shfl3(r.pos, src);
+    q.dir = shfl3(r.dir, src);
+    q.dpl = shfl3(r.dpl, src);
+    q.dpx = shfl3(r.dpx, src);
+    q.dpy = shfl3(r.dpy, src);
+    q.ddl = shfl3(r.ddl, src);
+    q.ddx = shfl3(r.ddx, src);
+    q.ddy = shfl3(r.ddy, src);
+    q.lam = __shfl_sync(kFull, r.lam, src);
+    q.x = __shfl_sync(kFull, r.x, src);
+    q.y = __shfl_sync(kFull, r.y, src);
+    q.ignore = __shfl_sync(kFull, r.ignore, src);
+    q.medium = __shfl_sync(kFull, r.medium, src);
+    return q;
+}
+
+// Sample s of a ray: s = ix + nd (iy + nd il), the CartesianIndices order of
+// atomic_spectrum_kernel2's threads.
+__device__ __forceinline__ bool sample_of(const SplatParams& sp, const RayState& q, const Tri& T, int s,
+                                          int64_t& off, float& inten) {
+    const int nd = sp.n_delta;
+    const int ix = s % nd;
+    const int iy = (s / nd) % nd;
+    const int il = s / (nd * nd);
+    const float lam = sp.n_lambda > 0 ? sp.spectrum[il] : q.lam;
+    const float xs = q.x + sp.deltas[ix];
+    const float ys = q.y + sp.deltas[iy];
+    int64_t oij;
+    if (!splat_sample(q, T, lam, xs, ys, sp.w, sp.h, oij, inten)) return false;
+    off = oij + (int64_t)il * sp.w * sp.h;
+    return true;
+}
+
+// All 32 lanes call; lanes with ok add their sample.
+__device__ __forceinline__ void accumulate_warp(const SplatParams& sp, bool ok, int64_t off, float inten) {
+    if (sp.accum == SPLAT_ACCUM_I32) {
+        const unsigned act = __ballot_sync(kFull, ok);
+        if (ok) {
+            const int v = __float2int_rn(inten * sp.scale);
+            const unsigned m = __match_any_sync(act, (unsigned long long)off);
+            const int sum = __reduce_add_sync(m, v);
+            if (lane_id() == __ffs(m) - 1) atomicAdd(reinterpret_cast<int*>(sp.map) + off, sum);
+        }
+    } else if (ok) {
+        atomicAdd(reinterpret_cast<float*>(sp.map) + off, inten);
+    }
+}
+
+__device__ __forceinline__ void accumulate_one(const SplatParams& sp, int64_t off, float inten) {
+    if (sp.accum == SPLAT_ACCUM_I32)
+        atomicAdd(reinterpret_cast<int*>(sp.map) + off, __float2int_rn(inten * sp.scale));
+    else
+        atomicAdd(reinterpret_cast<float*>(sp.map) + off, inten);
+}
+
+// Splat the diffuse rays held by the lanes of this warp (all lanes call).
+// Returns the number of samples this lane accumulated.
+__device__ __forceinline__ int splat_warp(const SplatParams& sp, const splat_ftri_t* tris, bool dif,
+                                          const RayState& fe, int32_t ti) {
+    const int S = (sp.n_lambda > 0 ? sp.n_lambda : 1) * sp.n_delta * sp.n_delta;
+    int done = 0;
+    if (S >= 8) {
+        unsigned dm = __ballot_sync(kFull, dif);
+        while (dm) {
+            const int src = __ffs(dm) - 1;
+            dm &= dm - 1;
+            const RayState q = shfl_ray(fe, src);
+            const int32_t qi = __shfl_sync(kFull, ti, src);
+            const Tri T = load_tri(tris, qi);
+            for (int s0 = 0; s0 < S; s0 += 32) {
+                const int s = s0 + lane_id();
+                bool ok = false;
+                int64_t off = 0;
+                float inten = 0.f;
+                if (s < S) ok = sample_of(sp, q, T, s, off, inten);
+                accumulate_warp(sp, ok, off, inten);
+                done += ok ? 1 : 0;
+            }
+        }
+    } else if (dif) {
+        const Tri T = load_tri(tris, ti);
+        for (int s = 0; s < S; ++s) {
+            int64_t off;
+            float inten;
+            if (sample_of(sp, fe, T, s, off, inten)) {
+                accumulate_one(sp, off, inten);
+                ++done;
+            }
+        }
+    }
+    return done;
+}
+
+__device__ __forceinline__ void add_stats(splat_trace_stats_t* st, int diffuse, int samples) {
+    if (!st) return;
+    const int d = __reduce_add_sync(kFull, diffuse);
+    const int s = __reduce_add_sync(kFull, samples);
+    if (lane_id() == 0) {
+        if (d) atomicAdd(reinterpret_cast<unsigned long long*>(&st->diffuse), (unsigned long long)d);
+        if (s) atomicAdd(reinterpret_cast<unsigned long long*>(&st->samples), (unsigned long long)s);
+    }
+}
+
+// TRACE: diffuse rays are final-evolved and splatted here, misses dropped, the
+// last bounce skips the optics.  PLUGIN: retired rays are written back to the
+// caller's AoS array with their status, as run_evolution! leaves them.
+template <bool TRACE>
+__global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
+    __shared__ int s_warp[kEvolveThreads / 32];
+    __shared__ unsigned long long s_base;
+    const int64_t n = *A.in_count;
+    const int lane = lane_id();
+    const int wid = threadIdx.x >> 5;
+    const bool quirks = A.quirks != 0;
+    for (int64_t base = (int64_t)blockIdx.x * kEvolveThreads; base < n; base += (int64_t)gridDim.x * kEvolveThreads) {
+        const int64_t k = base + threadIdx.x;
+        bool keep = false, dif = false;
+        RayState r, o;
+        uint32_t id = 0;
+        int32_t ih = 1;
+        if (k < n) {
+            r = load_ray(A.in, k);
+            id = A.in.id[k];
+            int32_t i = A.hit_idx[k];
+            if (i < 1 || i > A.n_tris) {
+                atomicOr(A.err, 16);
+                i = 1;
+            }
+            const Tri T = load_tri(A.tris, i);
+            HitDerivs h;
+            ih = get_hit_ad(r, i, T, h);
+            if (ih >= A.first_diffuse) {
+                dif = true;
+                if (TRACE) final_evolution(r, h, ih, o);
+                else ray_to_aos(A.aos[id], r, kStatusDiffuse);
+            } else if (isinf(h.t)) {
+                if (!TRACE) ray_to_aos(A.aos[id], r, kStatusInfinity);
+            } else if (!TRACE || !A.last) {
+                const float u = A.force_rand >= 0.0f ? A.force_rand : fresnel_draw(A.seed, id, A.bounce);
+                handle_optics(r, h, ih, T, A.material, u, quirks, o);
+                keep = true;
+            }
+        }
+        // compaction: ballot -> block scan -> one atomic per block
+        const unsigned kb = __ballot_sync(kFull, keep);
+        if (lane == 0) s_warp[wid] = __popc(kb);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tot = 0;
+            for (int w = 0; w < kEvolveThreads / 32; ++w) {
+                const int c = s_warp[w];
+                s_warp[w] = tot;
+                tot += c;
+            }
+            s_base = tot ? atomicAdd(reinterpret_cast<unsigned long long*>(A.out_count), (unsigned long long)tot) : 0ull;
+        }
+        __syncthreads();
+        if (keep) {
+            const int64_t pos = (int64_t)s_base + s_warp[wid] + __popc(kb & ((1u << lane) - 1u));
+            store_ray(A.out, pos, o, id);
+        }
+        if (TRACE) {
+            const int samples = splat_warp(A.sp, A.tris, dif, o, ih);
+            add_stats(A.stats, dif ? 1 : 0, samples);
+        }
+        __syncthreads();
+    }
+}
+
+static int evolve_grid(int64_t cap, int sm_count) {
+    int64_t b = (cap + kEvolveThreads - 1) / kEvolveThreads;
+    const int64_t lim = (int64_t)sm_count * 8;
+    if (b > lim) b = lim;
+    return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_evolve_trace(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s) {
+    if (cap <= 0) return cudaSuccess;
+    evolve_kernel<true><<<evolve_grid(cap, sm_count), kEvolveThreads, 0, s>>>(a);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_evolve_plugin(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s) {
+    if (cap <= 0) return cudaSuccess;
+    evolve_kernel<false><<<evolve_grid(cap, sm_count), kEvolveThreads, 0, s>>>(a);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+// continuum_light_map2! on the caller's AoS rays: final_evolution in place,
+// then the splat.
+__global__ void __launch_bounds__(kEvolveThreads) light_map_kernel(splat_adray_t* rays, int64_t n,
+                                                                   const int32_t* __restrict__ hit_idx,
+                                                                   const splat_ftri_t* __restrict__ tris,
+                                                                   int64_t n_tris, int32_t* err, SplatParams sp) {
+    for (int64_t base = (int64_t)blockIdx.x * kEvolveThreads; base < n; base += (int64_t)gridDim.x * kEvolveThreads) {
+        const int64_t k = base + threadIdx.x;
+        bool dif = false;
+        RayState o;
+        int32_t ih = 1;
+        if (k < n && rays[k].status == kStatusDiffuse) {
+            const int32_t i = hit_idx[k];
+            if (i >= 1 && i <= n_tris) {
+                const RayState r = ray_from_aos(rays[k]);
+                const Tri T = load_tri(tris, i);
+                HitDerivs h;
+                ih = get_hit_ad(r, i, T, h);
+                final_evolution(r, h, ih, o);
+                ray_to_aos(rays[k], o, kStatusDiffuse);
+                dif = true;
+            } else {
+                atomicOr(err, 16);
+            }
+        }
+        (void)splat_warp(sp, tris, dif, o, ih);
+    }
+}
+
+cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_idx, const splat_ftri_t* tris,
+                             int64_t n_tris, int32_t* err, const SplatParams& sp, int sm_count, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    light_map_kernel<<<evolve_grid(n, sm_count), kEvolveThreads, 0, s>>>(rays, n, hit_idx, tris, n_tris, err, sp);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+__global__ void stats_finish_kernel(const int64_t* counts, int depth, splat_trace_stats_t* st, const int32_t* err) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        for (int b = 0; b < 8; ++b) st->rays_per_bounce[b] = b < depth ? counts[b] : 0;
+        st->error = err ? *err : 0;
+    }
+}
+
+cudaError_t launch_stats_finish(const int64_t* counts, int depth, splat_trace_stats_t* stats, const int32_t* err,
+                                cudaStream_t s) {
+    stats_finish_kernel<<<1, 32, 0, s>>>(counts, depth, stats, err);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// ray generation, src/ray_generators.jl:64-97
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float gen_lambda(const splat_lambda_mode_t& lm, uint32_t k, float u) {
+    if (lm.mode == SPLAT_LAMBDA_UNIFORM) return lm.lambda0 + (lm.lambda1 - lm.lambda0) * u;
+    if (lm.mode == SPLAT_LAMBDA_STRATIFIED) {
+        const float width = (lm.lambda1 - lm.lambda0) / (float)lm.n_strata;
+        return lm.lambda0 + ((float)(k % (uint32_t)lm.n_strata) + u) * width;
+    }
+    return lm.lambda0;
+}
+
+__device__ __forceinline__ RayState gen_ray(const GenParams& g, int64_t kid) {
+    const int64_t h = g.light.res1 / g.upscale, w = g.light.res2 / g.upscale;
+    const int64_t row = kid % h + 1, col = kid / h + 1;
+    const uint4 rnd = philox(make_uint4((uint32_t)kid, g.light_index, 0u, 0u), (uint32_t)g.seed,
+                             (uint32_t)(g.seed >> 32));
+    const float ddx = uniform24(rnd.x), ddy = uniform24(rnd.y);
+    const float xf = (float)row + ddx, yf = (float)col + ddy;
+    const float h2 = (float)(h / 2), w2 = (float)(w / 2);
+    const F3 C = f3(g.light.center), d1 = f3(g.light.dim1), d2 = f3(g.light.dim2);
+    const float sx = xf - h2, sy = yf - w2;
+    const F3 A = {(d1.x * sx) / h2, (d1.y * sx) / h2, (d1.z * sx) / h2};
+    const F3 B = {(d2.x * sy) / w2, (d2.y * sy) / w2, (d2.z * sy) / w2};
+    RayState r;
+    r.pos = (C + A) + B;
+    r.dpl = {0.f, 0.f, 0.f};
+    r.dpx = {d1.x / h2, d1.y / h2, d1.z / h2};
+    r.dpy = {d2.x / w2, d2.y / w2, d2.z / w2};
+    r.dir = f3(g.light.dir);
+    r.ddl = {0.f, 0.f, 0.f};
+    r.ddx = {0.f, 0.f, 0.f};
+    r.ddy = {0.f, 0.f, 0.f};
+    r.lam = gen_lambda(g.lm, (uint32_t)kid, uniform24(rnd.z));
+    r.x = xf;
+    r.y = yf;
+    r.ignore = 1;
+    r.medium = 0;
+    return r;
+}
+
+__global__ void generate_soa_kernel(GenParams g, int64_t n, RaySoA out, int64_t* d_count) {
+    if (blockIdx.x == 0 && threadIdx.x == 0 && d_count) *d_count = n;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t kid = g.ray_begin + k;
+        store_ray(out, k, gen_ray(g, kid), (uint32_t)kid);
+    }
+}
+
+__global__ void generate_aos_kernel(GenParams g, int64_t n, splat_adray_t* out) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const RayState r = gen_ray(g, g.ray_begin + k);
+        splat_adray_t a;
+        memset(&a, 0, sizeof(a));
+        ray_to_aos(a, r, kStatusActive);
+        a.dest = 0;
+        out[k] = a;
+    }
+}
+
+cudaError_t launch_generate_soa(const GenParams& g, int64_t n, RaySoA out, int64_t* d_count, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    generate_soa_kernel<<<evolve_grid(n, 152), 256, 0, s>>>(g, n, out, d_count);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_generate_aos(const GenParams& g, int64_t n, splat_adray_t* out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    generate_aos_kernel<<<evolve_grid(n, 152), 256, 0, s>>>(g, n, out);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+// active AoS rays -> SoA (id = slot), compacted with one atomic per warp
+__global__ void aos_to_soa_kernel(const splat_adray_t* in, int64_t n, RaySoA out, int64_t* d_count) {
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = base + threadIdx.x;
+        const bool act = k < n && in[k].status == kStatusActive;
+        const unsigned b = __ballot_sync(kFull, act);
+        unsigned long long wbase = 0;
+        if (lane_id() == 0 && b)
+            wbase = atomicAdd(reinterpret_cast<unsigned long long*>(d_count), (unsigned long long)__popc(b));
+        wbase = __shfl_sync(kFull, wbase, 0);
+        if (act) {
+            const int64_t pos = (int64_t)wbase + __popc(b & ((1u << lane_id()) - 1u));
+            store_ray(out, pos, ray_from_aos(in[k]), (uint32_t)k);
+        }
+    }
+}
+
+__global__ void soa_to_aos_kernel(RaySoA in, const int64_t* d_count, splat_adray_t* out, int status) {
+    const int64_t n = *d_count;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        ray_to_aos(out[in.id[k]], load_ray(in, k), status);
+}
+
+cudaError_t launch_aos_to_soa(const splat_adray_t* in, int64_t n, RaySoA out, int64_t* d_count, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    aos_to_soa_kernel<<<evolve_grid(n, 152), 256, 0, s>>>(in, n, out, d_count);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_soa_to_aos(RaySoA in, const int64_t* d_count, splat_adray_t* out, int status, cudaStream_t s) {
+    if (in.cap <= 0) return cudaSuccess;
+    soa_to_aos_kernel<<<evolve_grid(in.cap, 152), 256, 0, s>>>(in, d_count, out, status);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+}  // namespace splat

@@ -1,0 +1,621 @@
+// hit.cu -- nearest-hit kernels.
+//
+// Semantics (src/hitters.jl:24-30, src/tracer.jl:45-59): for every ray, the
+// lexicographic minimum of (t, index) over the triangles with
+// in_triangle(o + d t) && t > 0 && index != ignore_tri; (Inf, 1) when none.
+// All kernels evaluate the reference's test with the same binary32
+// operations, so t and the index are bit-identical to the CPU restatement.
+//
+// * hit_brute_kernel: all pairs.  Hit records are staged through shared
+//   memory by TMA bulk copies (cp.async.bulk + mbarrier, 4-stage ring, no
+//   multicast); each thread keeps RPT rays in registers and their running
+//   argmin.  Triangle ranges split over blockIdx.y merge with a packed 64-bit
+//   atomicMin (src/atomic_argmin.jl).
+// * hit_bvh_kernel: one thread per ray walks the flattened BVH2 with a short
+//   per-thread stack; boxes are padded so every triangle whose test can
+//   succeed is visited, and the same lexicographic rule makes the result
+//   identical to brute force.
+#include <cstdio>
+
+#include "kernels.h"
+
+namespace splat {
+
+thread_local int64_t g_launches = 0;
+
+// ---------------------------------------------------------------------------
+// PTX helpers: mbarrier + bulk copy (sm_90+ async proxy)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: gives up after kWaitLimit polls (each poll may suspend the
+// thread for a hardware-chosen time), so a lost copy cannot hang the GPU.
+constexpr uint32_t kWaitLimit = 1u << 24;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase) {
+    for (uint32_t it = 0; it < kWaitLimit; ++it)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// ray loading
+// ---------------------------------------------------------------------------
+struct HitRay {
+    float ox, oy, oz, dx, dy, dz;
+    int32_t ig;
+};
+
+template <bool AOS>
+__device__ __forceinline__ HitRay load_hit_ray(const RaySrc& s, int64_t k) {
+    HitRay r;
+    if (AOS) {
+        const splat_adray_t& a = s.aos[k];
+        r.ox = a.pos[0];
+        r.oy = a.pos[1];
+        r.oz = a.pos[2];
+        r.dx = a.dir[0];
+        r.dy = a.dir[1];
+        r.dz = a.dir[2];
+        r.ig = (int32_t)a.ignore_tri;
+    } else {
+        const float* f = s.f;
+        const int64_t c = s.cap;
+        r.ox = f[k];
+        r.oy = f[c + k];
+        r.oz = f[2 * c + k];
+        r.dx = f[3 * c + k];
+        r.dy = f[4 * c + k];
+        r.dz = f[5 * c + k];
+        r.ig = s.ignore[k];
+    }
+    return r;
+}
+
+// The reference's test on one hoisted record (src/geo.jl:433-466).
+__device__ __forceinline__ float tri_t(const float4& q0, const float4& q1, const float4& q2, const float4& q3,
+                                       const float4& q4, const HitRay& r, bool& inside) {
+    float num = q0.w - ((q0.x * r.ox + q0.y * r.oy) + q0.z * r.oz);
+    float den = (q0.x * r.dx + q0.y * r.dy) + q0.z * r.dz;
+    float t = num / den;
+    float px = r.ox + r.dx * t;
+    float py = r.oy + r.dy * t;
+    float pz = r.oz + r.dz * t;
+    float v2x = px - q1.x, v2y = py - q1.y, v2z = pz - q1.z;
+    float d02 = (q2.x * v2x + q2.y * v2y) + q2.z * v2z;
+    float d12 = (q3.x * v2x + q3.y * v2y) + q3.z * v2z;
+    float u = (q3.w * d02 - q4.x * d12) * q4.y;
+    float v = (q2.w * d12 - q4.x * d02) * q4.y;
+    inside = (u >= 0.0f) & (v >= 0.0f) & (u + v < 1.0f);
+    return t;
+}
+
+// ---------------------------------------------------------------------------
+// brute force, TMA-staged tiles
+// ---------------------------------------------------------------------------
+constexpr int kBruteThreads = 256;
+constexpr int kTile = 64;
+constexpr int kStages = 4;
+
+template <int RPT, bool AOS>
+__global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, const TriHit* __restrict__ recs,
+                                                                  int64_t n_recs, int64_t per_split,
+                                                                  int32_t* __restrict__ hit_idx,
+                                                                  float* __restrict__ hit_t,
+                                                                  unsigned long long* __restrict__ tmp,
+                                                                  int32_t* err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TriHit* tiles = reinterpret_cast<TriHit*>(smem_raw);
+    __shared__ __align__(8) uint64_t bars[kStages];
+
+    const int64_t n = src.d_count ? *src.d_count : src.n;
+    const int64_t ray0 = (int64_t)blockIdx.x * kBruteThreads * RPT;
+    if (ray0 >= n) return;
+    const int64_t tb = (int64_t)blockIdx.y * per_split;
+    const int64_t te = min(n_recs, tb + per_split);
+    if (tb >= te) return;
+    const int n_tiles = (int)((te - tb + kTile - 1) / kTile);
+
+    HitRay ray[RPT];
+    float best[RPT];
+    int32_t bi[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        const int64_t k = ray0 + threadIdx.x + (int64_t)r * kBruteThreads;
+        if (k < n) {
+            ray[r] = load_hit_ray<AOS>(src, k);
+        } else {
+            ray[r] = HitRay{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
+        }
+        best[r] = __int_as_float(0x7f800000);
+        bi[r] = 1;
+    }
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](int kt) {
+        const int s = kt % kStages;
+        const int64_t first = tb + (int64_t)kt * kTile;
+        const uint32_t cnt = (uint32_t)min((int64_t)kTile, te - first);
+        const uint32_t bytes = cnt * (uint32_t)sizeof(TriHit);
+        mbar_arrive_expect_tx(&bars[s], bytes);
+        bulk_g2s(tiles + s * kTile, recs + first, bytes, &bars[s]);
+    };
+    if (threadIdx.x == 0) {
+        for (int kt = 0; kt < min(kStages, n_tiles); ++kt) issue(kt);
+    }
+
+    int consumed = 0;
+    bool failed = false;
+    for (int kt = 0; kt < n_tiles; ++kt) {
+        const int s = kt % kStages;
+        const uint32_t ph = (uint32_t)(kt / kStages) & 1u;
+        const bool ok = mbar_wait_bounded(&bars[s], ph);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        const int cnt = (int)min((int64_t)kTile, te - (tb + (int64_t)kt * kTile));
+        const TriHit* tile = tiles + s * kTile;
+#pragma unroll 2
+        for (int j = 0; j < cnt; ++j) {
+            const float4 q0 = tile[j].n_nv;
+            const float4 q1 = tile[j].a_idx;
+            const float4 q2 = tile[j].e0;
+            const float4 q3 = tile[j].e1;
+            const float4 q4 = tile[j].inv;
+            const int32_t idx = __float_as_int(q1.w);
+#pragma unroll
+            for (int r = 0; r < RPT; ++r) {
+                bool inside;
+                const float t = tri_t(q0, q1, q2, q3, q4, ray[r], inside);
+                if (inside & (t > 0.0f) & (idx != ray[r].ig) & (t < best[r])) {
+                    best[r] = t;
+                    bi[r] = idx;
+                }
+            }
+        }
+        consumed = kt + 1;
+        __syncthreads();
+        if (threadIdx.x == 0 && kt + kStages < n_tiles) {
+            fence_proxy_async();
+            issue(kt + kStages);
+        }
+    }
+    if (failed) {
+        if (threadIdx.x == 0) {
+            atomicOr(err, 1);
+            // drain this block's copies still in flight (bounded) before exit
+            const int issued = min(n_tiles, consumed + kStages);
+            for (int kt = consumed; kt < issued; ++kt)
+                (void)mbar_wait_bounded(&bars[kt % kStages], (uint32_t)(kt / kStages) & 1u);
+        }
+        return;
+    }
+
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) {
+        const int64_t k = ray0 + threadIdx.x + (int64_t)r * kBruteThreads;
+        if (k >= n) continue;
+        if (tmp) {
+            if (bi[r] != 1) atomicMin(tmp + k, (unsigned long long)pack_argmin(best[r], (uint32_t)bi[r]));
+        } else {
+            hit_idx[k] = bi[r];
+            if (hit_t) hit_t[k] = best[r];
+        }
+    }
+}
+
+__global__ void fill_u64_kernel(unsigned long long* p, int64_t n, const int64_t* d_count, unsigned long long v) {
+    const int64_t m = d_count ? *d_count : n;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x)
+        p[k] = v;
+}
+
+__global__ void unpack_hits_kernel(const unsigned long long* tmp, int64_t n, const int64_t* d_count,
+                                   int32_t* hit_idx, float* hit_t) {
+    const int64_t m = d_count ? *d_count : n;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = tmp[k];
+        hit_idx[k] = (int32_t)(uint32_t)(v & 0xffffffffull);
+        if (hit_t) hit_t[k] = monotonic_f32((uint32_t)(v >> 32));
+    }
+}
+
+__global__ void miss_kernel(int64_t n, const int64_t* d_count, int32_t* hit_idx, float* hit_t) {
+    const int64_t m = d_count ? *d_count : n;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x) {
+        hit_idx[k] = 1;
+        if (hit_t) hit_t[k] = __int_as_float(0x7f800000);
+    }
+}
+
+static int grid_for(int64_t n, int threads, int sm_count, int per_sm) {
+    int64_t b = (n + threads - 1) / threads;
+    int64_t cap = (int64_t)sm_count * per_sm;
+    if (b > cap) b = cap;
+    return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_unpack_hits(const uint64_t* tmp, int64_t n, const int64_t* d_count, int32_t* hit_idx,
+                               float* hit_t, cudaStream_t s) {
+    unpack_hits_kernel<<<grid_for(n, 256, 152, 8), 256, 0, s>>>((const unsigned long long*)tmp, n, d_count, hit_idx,
+                                                                hit_t);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+constexpr int kRPT = 2;
+
+cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs, int64_t n_recs, int32_t* hit_idx,
+                             float* hit_t, uint64_t* tmp, int32_t* err, int sm_count, cudaStream_t s) {
+    if (cap <= 0) return cudaSuccess;
+    const int64_t rays_per_block = (int64_t)kBruteThreads * kRPT;
+    const int64_t ray_blocks = (cap + rays_per_block - 1) / rays_per_block;
+    // split the triangle range so the grid covers the GPU a few times over
+    int64_t splits = ((int64_t)sm_count * 4 + ray_blocks - 1) / ray_blocks;
+    const int64_t max_splits = (n_recs + 4 * kTile - 1) / (4 * kTile);
+    if (splits > max_splits) splits = max_splits;
+    if (splits < 1) splits = 1;
+    if (splits > 65535) splits = 65535;
+    if (tmp == nullptr) splits = 1;
+    int64_t per_split = (n_recs + splits - 1) / splits;
+    per_split = ((per_split + kTile - 1) / kTile) * kTile;
+    splits = (n_recs + per_split - 1) / per_split;
+    if (splits < 1) splits = 1;
+    const size_t smem = (size_t)kStages * kTile * sizeof(TriHit);
+    const bool use_tmp = splits > 1;
+    if (use_tmp) {
+        fill_u64_kernel<<<grid_for(cap, 256, sm_count, 8), 256, 0, s>>>((unsigned long long*)tmp, cap, rays.d_count,
+                                                                        (unsigned long long)kNoHit);
+        ++g_launches;
+    }
+    dim3 grid((unsigned)ray_blocks, (unsigned)splits);
+    if (n_recs > 0) {
+        if (rays.aos)
+            hit_brute_kernel<kRPT, true><<<grid, kBruteThreads, smem, s>>>(
+                rays, recs, n_recs, per_split, hit_idx, hit_t, use_tmp ? (unsigned long long*)tmp : nullptr, err);
+        else
+            hit_brute_kernel<kRPT, false><<<grid, kBruteThreads, smem, s>>>(
+                rays, recs, n_recs, per_split, hit_idx, hit_t, use_tmp ? (unsigned long long*)tmp : nullptr, err);
+        ++g_launches;
+    } else {
+        // no triangles: every ray misses
+        miss_kernel<<<grid_for(cap, 256, sm_count, 8), 256, 0, s>>>(cap, rays.d_count, hit_idx, hit_t);
+        ++g_launches;
+        return cudaGetLastError();
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (use_tmp) return launch_unpack_hits(tmp, cap, rays.d_count, hit_idx, hit_t, s);
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// brute force over the reference's n_tris array (next_hit_kernel6 drop-in)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ TriHit pack_one(int32_t idx, F3 n, F3 a, F3 b, F3 c) {
+    TriHit h;
+    F3 v0 = c - a, v1 = b - a;
+    float dot00 = dot(v0, v0), dot01 = dot(v0, v1), dot11 = dot(v1, v1);
+    float invDenom = 1.0f / (dot00 * dot11 - dot01 * dot01);
+    h.n_nv = make_float4(n.x, n.y, n.z, dot(n, a));
+    h.a_idx = make_float4(a.x, a.y, a.z, __int_as_float(idx));
+    h.e0 = make_float4(v0.x, v0.y, v0.z, dot00);
+    h.e1 = make_float4(v1.x, v1.y, v1.z, dot11);
+    h.inv = make_float4(dot01, invDenom, 0.f, 0.f);
+    return h;
+}
+
+__global__ void __launch_bounds__(kBruteThreads) hit_ntris_kernel(const splat_adray_t* __restrict__ rays,
+                                                                   int64_t n_rays, const splat_ntri_t* __restrict__ nt,
+                                                                   int64_t n_tris, int64_t per_split,
+                                                                   unsigned long long* __restrict__ tmp) {
+    __shared__ TriHit tile[kTile];
+    RaySrc src{};
+    src.aos = rays;
+    src.n = n_rays;
+    const int64_t ray0 = (int64_t)blockIdx.x * kBruteThreads * kRPT;
+    const int64_t tb = (int64_t)blockIdx.y * per_split;
+    const int64_t te = min(n_tris, tb + per_split);
+    if (tb >= te) return;
+    HitRay ray[kRPT];
+    float best[kRPT];
+    int32_t bi[kRPT];
+#pragma unroll
+    for (int r = 0; r < kRPT; ++r) {
+        const int64_t k = ray0 + threadIdx.x + (int64_t)r * kBruteThreads;
+        ray[r] = k < n_rays ? load_hit_ray<true>(src, k) : HitRay{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
+        best[r] = __int_as_float(0x7f800000);
+        bi[r] = 1;
+    }
+    for (int64_t base = tb; base < te; base += kTile) {
+        const int cnt = (int)min((int64_t)kTile, te - base);
+        if (threadIdx.x < cnt) {
+            const splat_ntri_t& q = nt[base + threadIdx.x];
+            tile[threadIdx.x] = pack_one(q.idx, f3(q.v[0]), f3(q.v[1]), f3(q.v[2]), f3(q.v[3]));
+        }
+        __syncthreads();
+        for (int j = 0; j < cnt; ++j) {
+            const float4 q0 = tile[j].n_nv, q1 = tile[j].a_idx, q2 = tile[j].e0, q3 = tile[j].e1, q4 = tile[j].inv;
+            const int32_t idx = __float_as_int(q1.w);
+#pragma unroll
+            for (int r = 0; r < kRPT; ++r) {
+                bool inside;
+                const float t = tri_t(q0, q1, q2, q3, q4, ray[r], inside);
+                // next_hit_kernel6 (src/hitters.jl:183) has no i != 1 test: the
+                // sentinel's t is NaN and fails t > 0.
+                if (inside & (t > 0.0f) & (idx != ray[r].ig) & (t < best[r])) {
+                    best[r] = t;
+                    bi[r] = idx;
+                }
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < kRPT; ++r) {
+        const int64_t k = ray0 + threadIdx.x + (int64_t)r * kBruteThreads;
+        if (k < n_rays && bi[r] != 1) atomicMin(tmp + k, (unsigned long long)pack_argmin(best[r], (uint32_t)bi[r]));
+    }
+}
+
+cudaError_t launch_hit_brute_ntris(const splat_adray_t* rays, int64_t n_rays, const splat_ntri_t* ntris,
+                                   int64_t n_tris, uint64_t* tmp, int32_t* hit_idx, int sm_count, cudaStream_t s) {
+    if (n_rays <= 0) return cudaSuccess;
+    fill_u64_kernel<<<grid_for(n_rays, 256, sm_count, 8), 256, 0, s>>>((unsigned long long*)tmp, n_rays, nullptr,
+                                                                       (unsigned long long)kNoHit);
+    ++g_launches;
+    const int64_t rays_per_block = (int64_t)kBruteThreads * kRPT;
+    const int64_t ray_blocks = (n_rays + rays_per_block - 1) / rays_per_block;
+    int64_t splits = ((int64_t)sm_count * 4 + ray_blocks - 1) / ray_blocks;
+    const int64_t max_splits = (n_tris + 4 * kTile - 1) / (4 * kTile);
+    if (splits > max_splits) splits = max_splits;
+    if (splits < 1) splits = 1;
+    if (splits > 65535) splits = 65535;
+    int64_t per_split = (n_tris + splits - 1) / splits;
+    per_split = ((per_split + kTile - 1) / kTile) * kTile;
+    if (per_split < kTile) per_split = kTile;
+    splits = (n_tris + per_split - 1) / per_split;
+    if (n_tris > 0) {
+        dim3 grid((unsigned)ray_blocks, (unsigned)splits);
+        hit_ntris_kernel<<<grid, kBruteThreads, 0, s>>>(rays, n_rays, ntris, n_tris, per_split,
+                                                         (unsigned long long*)tmp);
+        ++g_launches;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return launch_unpack_hits(tmp, n_rays, nullptr, hit_idx, nullptr, s);
+}
+
+// ---------------------------------------------------------------------------
+// BVH traversal
+// ---------------------------------------------------------------------------
+constexpr int kBvhThreads = 128;
+
+__device__ __forceinline__ float safe_inv(float d) {
+    return 1.0f / (fabsf(d) > 1.0e-30f ? d : copysignf(1.0e-30f, d));
+}
+
+template <bool AOS>
+__global__ void __launch_bounds__(kBvhThreads) hit_bvh_kernel(RaySrc src, BvhView bvh, int32_t* __restrict__ hit_idx,
+                                                              float* __restrict__ hit_t, int32_t* err) {
+    const int64_t n = src.d_count ? *src.d_count : src.n;
+    int stack_ref[kBvhStack];
+    float stack_t[kBvhStack];
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const HitRay r = load_hit_ray<AOS>(src, k);
+        const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
+        const float oix = r.ox * ix, oiy = r.oy * iy, oiz = r.oz * iz;
+        float best = __int_as_float(0x7f800000);
+        int32_t bi = 1;
+        int sp = 0;
+        int ref = 0;
+        while (true) {
+            if (ref >= 0) {
+                const BvhNode* nd = bvh.nodes + ref;
+                const float4 bx = __ldg(&nd->x);
+                const float4 by = __ldg(&nd->y);
+                const float4 bz = __ldg(&nd->z);
+                const int4 c = __ldg(&nd->c);
+                const float a0 = fmaf(bx.x, ix, -oix), b0 = fmaf(bx.y, ix, -oix);
+                const float a1 = fmaf(by.x, iy, -oiy), b1 = fmaf(by.y, iy, -oiy);
+                const float a2 = fmaf(bz.x, iz, -oiz), b2 = fmaf(bz.y, iz, -oiz);
+                const float tmin0 = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fminf(a2, b2));
+                const float tmax0 = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fmaxf(a2, b2));
+                const float e0 = fmaf(bx.z, ix, -oix), f0 = fmaf(bx.w, ix, -oix);
+                const float e1 = fmaf(by.z, iy, -oiy), f1 = fmaf(by.w, iy, -oiy);
+                const float e2 = fmaf(bz.z, iz, -oiz), f2 = fmaf(bz.w, iz, -oiz);
+                const float tmin1 = fmaxf(fmaxf(fminf(e0, f0), fminf(e1, f1)), fminf(e2, f2));
+                const float tmax1 = fminf(fminf(fmaxf(e0, f0), fmaxf(e1, f1)), fmaxf(e2, f2));
+                const bool h0 = (tmin0 <= tmax0) & (tmax0 >= 0.0f) & (tmin0 <= best);
+                const bool h1 = (tmin1 <= tmax1) & (tmax1 >= 0.0f) & (tmin1 <= best);
+                if (h0 && h1) {
+                    int near_ref = c.x, far_ref = c.y;
+                    float far_t = tmin1;
+                    if (tmin1 < tmin0) {
+                        near_ref = c.y;
+                        far_ref = c.x;
+                        far_t = tmin0;
+                    }
+                    if (sp < kBvhStack) {
+                        stack_ref[sp] = far_ref;
+                        stack_t[sp] = far_t;
+                        ++sp;
+                    } else {
+                        atomicOr(err, 2);
+                    }
+                    ref = near_ref;
+                    continue;
+                }
+                if (h0) {
+                    ref = c.x;
+                    continue;
+                }
+                if (h1) {
+                    ref = c.y;
+                    continue;
+                }
+            } else {
+                const int enc = ~ref;
+                const int first = enc >> 4;
+                const int count = (enc & 15) + 1;
+                for (int j = 0; j < count; ++j) {
+                    const TriHit* h = bvh.tris + first + j;
+                    const float4 q0 = __ldg(&h->n_nv), q1 = __ldg(&h->a_idx), q2 = __ldg(&h->e0),
+                                 q3 = __ldg(&h->e1), q4 = __ldg(&h->inv);
+                    const int32_t idx = __float_as_int(q1.w);
+                    bool inside;
+                    const float t = tri_t(q0, q1, q2, q3, q4, r, inside);
+                    if (inside & (t > 0.0f) & (idx != r.ig) & ((t < best) | ((t == best) & (idx < bi)))) {
+                        best = t;
+                        bi = idx;
+                    }
+                }
+            }
+            bool found = false;
+            while (sp > 0) {
+                --sp;
+                if (stack_t[sp] <= best) {
+                    ref = stack_ref[sp];
+                    found = true;
+                    break;
+                }
+            }
+            if (!found) break;
+        }
+        hit_idx[k] = bi;
+        if (hit_t) hit_t[k] = best;
+    }
+}
+
+cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, int32_t* hit_idx, float* hit_t,
+                           int32_t* err, int sm_count, cudaStream_t s) {
+    if (cap <= 0) return cudaSuccess;
+    const int grid = grid_for(cap, kBvhThreads, sm_count, 16);
+    if (rays.aos)
+        hit_bvh_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
+    else
+        hit_bvh_kernel<false><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// scene packing and BVH refit
+// ---------------------------------------------------------------------------
+__global__ void pack_hits_kernel(const splat_ftri_t* __restrict__ ftri, int64_t n_tris, TriHit* brute,
+                                 const int32_t* __restrict__ bvh_order, TriHit* bvh) {
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j + 1 < n_tris;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        // brute record j <- reference index j + 2 (the sentinel is never hit)
+        const float* p = ftri[j + 1].v[0];
+        brute[j] = pack_one((int32_t)(j + 2), f3(p), f3(p + 3), f3(p + 6), f3(p + 9));
+        if (bvh) {
+            const int32_t idx = bvh_order[j];
+            const float* q = ftri[idx - 1].v[0];
+            bvh[j] = pack_one(idx, f3(q), f3(q + 3), f3(q + 6), f3(q + 9));
+        }
+    }
+}
+
+cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, const int32_t* bvh_order,
+                             TriHit* bvh_recs, cudaStream_t s) {
+    if (n_tris <= 1) return cudaSuccess;
+    pack_hits_kernel<<<grid_for(n_tris, 256, 152, 8), 256, 0, s>>>(ftri, n_tris, brute_recs, bvh_order, bvh_recs);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+// Box of one child reference.  Leaf boxes are the padded vertex boxes of
+// their triangles; inner boxes are the union of the child node's two boxes.
+__device__ __forceinline__ void child_box(const BvhNode* nodes, int ref, const TriHit* recs,
+                                          const splat_ftri_t* ftri, float pad_abs, float pad_rel, float lo[3],
+                                          float hi[3]) {
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = __int_as_float(0x7f800000);
+        hi[a] = -__int_as_float(0x7f800000);
+    }
+    if (ref >= 0) {
+        const BvhNode& nd = nodes[ref];
+        lo[0] = fminf(nd.x.x, nd.x.z);
+        hi[0] = fmaxf(nd.x.y, nd.x.w);
+        lo[1] = fminf(nd.y.x, nd.y.z);
+        hi[1] = fmaxf(nd.y.y, nd.y.w);
+        lo[2] = fminf(nd.z.x, nd.z.z);
+        hi[2] = fmaxf(nd.z.y, nd.z.w);
+        return;
+    }
+    const int enc = ~ref;
+    const int first = enc >> 4, count = (enc & 15) + 1;
+    for (int j = 0; j < count; ++j) {
+        const int32_t idx = __float_as_int(recs[first + j].a_idx.w);
+        const float* p = ftri[idx - 1].v[1];
+        float tl[3], th[3];
+        for (int a = 0; a < 3; ++a) {
+            tl[a] = fminf(fminf(p[a], p[3 + a]), p[6 + a]);
+            th[a] = fmaxf(fmaxf(p[a], p[3 + a]), p[6 + a]);
+        }
+        const float dx = th[0] - tl[0], dy = th[1] - tl[1], dz = th[2] - tl[2];
+        const float pad = pad_abs + pad_rel * sqrtf(dx * dx + dy * dy + dz * dz);
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], tl[a] - pad);
+            hi[a] = fmaxf(hi[a], th[a] + pad);
+        }
+    }
+}
+
+__global__ void refit_level_kernel(BvhNode* nodes, const int32_t* __restrict__ level_nodes, int64_t n_level,
+                                   const TriHit* __restrict__ recs, const splat_ftri_t* __restrict__ ftri,
+                                   float pad_abs, float pad_rel) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n_level; q += (int64_t)gridDim.x * blockDim.x) {
+        BvhNode& nd = nodes[level_nodes[q]];
+        float l0[3], h0[3], l1[3], h1[3];
+        child_box(nodes, nd.c.x, recs, ftri, pad_abs, pad_rel, l0, h0);
+        child_box(nodes, nd.c.y, recs, ftri, pad_abs, pad_rel, l1, h1);
+        nd.x = make_float4(l0[0], h0[0], l1[0], h1[0]);
+        nd.y = make_float4(l0[1], h0[1], l1[1], h1[1]);
+        nd.z = make_float4(l0[2], h0[2], l1[2], h1[2]);
+    }
+}
+
+cudaError_t launch_refit_level(BvhNode* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,
+                               const splat_ftri_t* ftri, float pad_abs, float pad_rel, cudaStream_t s) {
+    if (n_level <= 0) return cudaSuccess;
+    refit_level_kernel<<<grid_for(n_level, 128, 152, 8), 128, 0, s>>>(nodes, level_nodes, n_level, bvh_recs, ftri,
+                                                                       pad_abs, pad_rel);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+}  // namespace splat

@@ -1,0 +1,113 @@
+// kernels.h -- host-side launchers shared by the translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace splat {
+
+// Kernels launched by this thread (for launch profiling).
+extern thread_local int64_t g_launches;
+
+// Where a hit kernel reads its rays: the structure-of-arrays bounce state
+// (count on the device) or the reference's AoS ADRay array.
+struct RaySrc {
+    const float* f;          // SoA planes (nullptr for AoS)
+    const int32_t* ignore;
+    int64_t cap;
+    const splat_adray_t* aos;  // AoS rays (nullptr for SoA)
+    const int64_t* d_count;    // active count on the device (SoA)
+    int64_t n;                 // ray count when d_count is null
+};
+
+// Flattened BVH2 node (Aila & Laine 2009 layout): the boxes of both children
+// and their references.  ref >= 0: inner node index; ref < 0: leaf,
+// ~ref = first << 4 | (count - 1) in the BVH-ordered hit-record array.
+struct __align__(16) BvhNode {
+    float4 x;  // c0.lo.x, c0.hi.x, c1.lo.x, c1.hi.x
+    float4 y;
+    float4 z;
+    int4 c;    // ref0, ref1, 0, 0
+};
+static_assert(sizeof(BvhNode) == 64, "BvhNode layout");
+
+constexpr int kLeafMax = 16;
+constexpr int kBvhStack = 64;
+
+struct BvhView {
+    const BvhNode* nodes;
+    const TriHit* tris;  // BVH order
+};
+
+// brute force over prepacked hit records (reference indices 2..T in order)
+cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs, int64_t n_recs, int32_t* hit_idx,
+                             float* hit_t, uint64_t* tmp, int32_t* err, int sm_count, cudaStream_t s);
+// brute force over the reference's n_tris array (Tuple{Int32,Tri})
+cudaError_t launch_hit_brute_ntris(const splat_adray_t* rays, int64_t n_rays, const splat_ntri_t* ntris,
+                                   int64_t n_tris, uint64_t* tmp, int32_t* hit_idx, int sm_count, cudaStream_t s);
+cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, int32_t* hit_idx, float* hit_t,
+                           int32_t* err, int sm_count, cudaStream_t s);
+
+// scene packing / refit
+cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, const int32_t* bvh_order,
+                             TriHit* bvh_recs, cudaStream_t s);
+cudaError_t launch_refit_level(BvhNode* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,
+                               const splat_ftri_t* ftri, float pad_abs, float pad_rel, cudaStream_t s);
+
+// generation and conversion
+struct GenParams {
+    splat_rect_light_t light;
+    int64_t upscale;
+    splat_lambda_mode_t lm;
+    uint64_t seed;
+    uint32_t light_index;
+    int64_t ray_begin;
+};
+cudaError_t launch_generate_soa(const GenParams& g, int64_t n, RaySoA out, int64_t* d_count, cudaStream_t s);
+cudaError_t launch_generate_aos(const GenParams& g, int64_t n, splat_adray_t* out, cudaStream_t s);
+cudaError_t launch_aos_to_soa(const splat_adray_t* in, int64_t n, RaySoA out, int64_t* d_count, cudaStream_t s);
+cudaError_t launch_soa_to_aos(RaySoA in, const int64_t* d_count, splat_adray_t* out, int status, cudaStream_t s);
+
+// evolve (+ compaction, + fused splat in trace mode)
+struct SplatParams {
+    void* map;
+    int32_t accum;  // SPLAT_ACCUM_*
+    float scale;    // 2^frac_bits
+    int64_t w, h;
+    int32_t n_lambda;  // 0: own wavelength
+    int32_t n_delta;
+    float spectrum[SPLAT_MAX_LAMBDA];
+    float deltas[16];
+};
+
+struct EvolveArgs {
+    RaySoA in, out;
+    const int64_t* in_count;
+    int64_t* out_count;
+    const int32_t* hit_idx;
+    const splat_ftri_t* tris;
+    int64_t n_tris;         // hit indices outside 1..n_tris are reported and treated as misses
+    int32_t* err;           // error word (bit 4: bad hit index)
+    int64_t first_diffuse;
+    splat_material_t material;
+    uint64_t seed;
+    uint32_t bounce;
+    float force_rand;
+    int32_t quirks;
+    int32_t last;           // trace mode: last bounce, no optics
+    splat_adray_t* aos;     // plugin mode: retired rays written back here
+    SplatParams sp;
+    splat_trace_stats_t* stats;
+};
+cudaError_t launch_evolve_trace(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s);
+cudaError_t launch_evolve_plugin(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s);
+cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_idx, const splat_ftri_t* tris,
+                             int64_t n_tris, int32_t* err, const SplatParams& sp, int sm_count, cudaStream_t s);
+cudaError_t launch_stats_finish(const int64_t* counts, int depth, splat_trace_stats_t* stats, const int32_t* err,
+                                cudaStream_t s);
+cudaError_t launch_unpack_hits(const uint64_t* tmp, int64_t n, const int64_t* d_count, int32_t* hit_idx,
+                               float* hit_t, cudaStream_t s);
+
+}  // namespace splat

@@ -1,0 +1,286 @@
+// optics.cuh -- evolve_ray, final_evolution and the light-map sample on one
+// ray, as device functions.
+//
+// The primal computation follows the reference expression by expression
+// (src/tracer.jl:61-201, src/ray_imagers.jl:4-113, src/geo.jl:170-561),
+// including its zero-offset expansions (pos + dp/dlambda * 0 + ...), whose
+// NaN / signed-zero behaviour the reference's results depend on.
+//
+// Derivatives: every ForwardDiff.derivative(f, a) of the reference becomes
+// one evaluation of f with the differentiated argument a dual (struct D) and
+// everything else plain float.  The operand types therefore mirror the
+// reference closures exactly (a normal held at r.lambda stays a float, air()
+// of a dual wavelength is a dual with zero partial), which is what makes the
+// partials -- and through them the fixed-point light map -- reproducible.
+#pragma once
+
+#include "common.cuh"
+
+namespace splat {
+
+// ----------------------------------------------------------------------------
+// materials, src/material.jl:1-13
+// ----------------------------------------------------------------------------
+template <class L>
+__device__ __forceinline__ L glass(const splat_material_t& m, L lam) {
+    if (m.kind == SPLAT_MATERIAL_CAUCHY) {
+        L lu = lam * 1.0e-3f;
+        return m.a + m.b / (lu * lu);
+    }
+    if (m.kind == SPLAT_MATERIAL_SELLMEIER) {
+        L lu = lam * 1.0e-3f;
+        L l2 = lu * lu;
+        L t0 = (m.sb[0] * l2) / (l2 - m.sc[0]);
+        L t1 = (m.sb[1] * l2) / (l2 - m.sc[1]);
+        L t2 = (m.sb[2] * l2) / (l2 - m.sc[2]);
+        L acc = 1.0f + t0;
+        acc = acc + t1;
+        acc = acc + t2;
+        return dsqrt(acc);
+    }
+    const float l1 = 400.0f, l2 = 700.0f, g1 = 1.3f, g2 = 1.4f;
+    const float slope = (g2 - g1) / (l2 - l1);
+    return slope * (lam - l1) + g1;
+}
+__device__ __forceinline__ float air(float) { return 1.0f; }
+__device__ __forceinline__ D air(D) { return {1.0f, 0.0f}; }
+
+// ----------------------------------------------------------------------------
+// expansions, src/geo.jl:398-410 and src/tracer.jl:109-116
+// ----------------------------------------------------------------------------
+template <class L, class X, class Y>
+__device__ __forceinline__ auto p_expansion(const RayState& r, L lam, X x, Y y) {
+    auto dl = lam - r.lam;
+    auto dx = x - r.x;
+    auto dy = y - r.y;
+    auto a0 = r.pos + r.dpl * dl;
+    auto a1 = a0 + r.dpx * dx;
+    return a1 + r.dpy * dy;
+}
+
+template <class L, class X, class Y>
+__device__ __forceinline__ auto d_expansion(const RayState& r, L lam, X x, Y y) {
+    auto dl = lam - r.lam;
+    auto dx = x - r.x;
+    auto dy = y - r.y;
+    auto a0 = r.dir + r.ddl * dl;
+    auto a1 = a0 + r.ddx * dx;
+    return a1 + r.ddy * dy;
+}
+
+struct HitDerivs {
+    float t, dtl, dtx, dty;
+};
+
+template <class L, class X, class Y>
+__device__ __forceinline__ auto next_p(const RayState& r, const HitDerivs& h, L lam, X x, Y y) {
+    auto dl = lam - r.lam;
+    auto dx = x - r.x;
+    auto dy = y - r.y;
+    auto s0 = h.t + h.dtl * dl;
+    auto s1 = s0 + h.dtx * dx;
+    auto s = s1 + h.dty * dy;
+    return p_expansion(r, lam, x, y) + d_expansion(r, lam, x, y) * s;
+}
+
+// distance_to_plane(r, T, lambda, x, y), src/geo.jl:441-443
+template <class L, class X, class Y>
+__device__ __forceinline__ auto distance_to_plane_d(const RayState& r, const Tri& T, L lam, X x, Y y) {
+    auto o = p_expansion(r, lam, x, y);
+    auto d = d_expansion(r, lam, x, y);
+    auto num = dot(T.n, T.a) - dot(T.n, o);
+    return num / dot(T.n, d);
+}
+
+// src/geo.jl:446-466 (Blackpawn)
+__device__ __forceinline__ bool in_triangle(F3 p, F3 a, F3 b, F3 c) {
+    F3 v0 = c - a;
+    F3 v1 = b - a;
+    F3 v2 = p - a;
+    float dot00 = dot(v0, v0);
+    float dot01 = dot(v0, v1);
+    float dot02 = dot(v0, v2);
+    float dot11 = dot(v1, v1);
+    float dot12 = dot(v1, v2);
+    float invDenom = 1.0f / (dot00 * dot11 - dot01 * dot01);
+    float u = (dot11 * dot02 - dot01 * dot12) * invDenom;
+    float v = (dot00 * dot12 - dot01 * dot02) * invDenom;
+    return (u >= 0.0f) && (v >= 0.0f) && (u + v < 1.0f);
+}
+
+// get_hit(::Tuple{Int32,Tri}, ::ADRay), src/tracer.jl:61-81.  Returns the
+// index (1 on a miss) and t with its three partials (Inf on a miss).
+__device__ __forceinline__ int32_t get_hit_ad(const RayState& r, int32_t i, const Tri& T, HitDerivs& h) {
+    float t0 = (dot(T.n, T.a) - dot(T.n, r.pos)) / dot(T.n, r.dir);
+    F3 p0 = r.pos + r.dir * t0;
+    if (in_triangle(p0, T.a, T.b, T.c) && t0 > 0.0f && r.ignore != i) {
+        h.t = t0;
+        h.dtl = distance_to_plane_d(r, T, D{r.lam, 1.0f}, r.x, r.y).d;
+        h.dtx = distance_to_plane_d(r, T, r.lam, D{r.x, 1.0f}, r.y).d;
+        h.dty = distance_to_plane_d(r, T, r.lam, r.x, D{r.y, 1.0f}).d;
+        return i;
+    }
+    h.t = h.dtl = h.dtx = h.dty = __int_as_float(0x7f800000);
+    return 1;
+}
+
+// reverse_uv, src/geo.jl:232-258
+template <class P>
+__device__ __forceinline__ void reverse_uv(V3<P> pos, const Tri& T, P& u, P& v) {
+    F3 v0v1 = T.b - T.a;
+    F3 v0v2 = T.c - T.a;
+    F3 N = cross(v0v1, v0v2);
+    float denom = dot(N, N);
+    F3 edge1 = T.c - T.b;
+    auto C1 = cross(edge1, pos - T.b);
+    P uu = dot(N, C1);
+    F3 edge2 = T.a - T.c;
+    auto C2 = cross(edge2, pos - T.c);
+    P vv = dot(N, C2);
+    u = uu / denom;
+    v = vv / denom;
+}
+
+// optical_normal(::STri, pos), src/geo.jl:202-212
+template <class P>
+__device__ __forceinline__ V3<P> optical_normal(const Tri& T, V3<P> pos) {
+    P u, v;
+    reverse_uv(pos, T, u, v);
+    P w = (1.0f - u) - v;
+    auto n = (T.na * u + T.nb * v) + T.nc * w;
+    return normalize(n);
+}
+
+template <class L, class X, class Y>
+__device__ __forceinline__ auto N_at(const RayState& r, const HitDerivs& h, const Tri& T, L lam, X x, Y y) {
+    return optical_normal(T, next_p(r, h, lam, x, y));
+}
+
+// refract, src/geo.jl:548-561 (the sign convention of c1 as written)
+template <class A, class B, class C1, class C2>
+__device__ __forceinline__ auto refract(V3<A> v, V3<B> normal, C1 n1, C2 n2) {
+    V3<B> n = normalize(normal);
+    if (val(dot(v, n)) > 0.0f) n = n * -1.0f;
+    auto c1 = dot(normalize(v), n);
+    auto s1 = dsqrt(1.0f - c1 * c1);
+    auto s2 = (n1 / n2) * s1;
+    auto c2 = dsqrt(1.0f - s2 * s2);
+    auto k = (n1 / n2) * c1 - c2;
+    return normalize(v * (n1 / n2) + n * k);
+}
+
+// reflect, src/geo.jl:481-486
+template <class A, class B>
+__device__ __forceinline__ auto reflect(V3<A> v, V3<B> normal) {
+    V3<B> n = normalize(normal);
+    auto dd = dot(n, v);
+    auto ax = (n.x * dd) * 2.0f;
+    auto ay = (n.y * dd) * 2.0f;
+    auto az = (n.z * dd) * 2.0f;
+    return V3<decltype(v.x - ax)>{v.x - ax, v.y - ay, v.z - az};
+}
+
+// can_refract, src/geo.jl:528-542 (1 - 1f-9 rounds to 1f0)
+__device__ __forceinline__ bool can_refract(F3 v, F3 normal, float n1, float n2) {
+    F3 n = normalize(normal);
+    if (dot(n, v) > 0.0f) n = n * -1.0f;
+    float c1 = dot(normalize(v), n);
+    const float one_m_eps = 1.0f - 1.0e-9f;
+    if (c1 * c1 > one_m_eps) return false;
+    float s1 = sqrtf(1.0f - c1 * c1);
+    float s2 = (n1 / n2) * s1;
+    return fabsf(s2) < one_m_eps;
+}
+
+// reflectance, src/geo.jl:488-502
+__device__ __forceinline__ float reflectance(F3 v, F3 normal, float n1, float n2) {
+    F3 n = normalize(normal);
+    if (dot(n, v) < 0.0f) n = n * -1.0f;
+    float c1 = dot(normalize(v), n);
+    float s1 = sqrtf(1.0f - c1 * c1);
+    float r = n1 / n2;
+    float s2 = sqrtf(1.0f - (r * r) * (s1 * s1));
+    float hh = (n1 + n2) / 2.0f;
+    float q = (hh * c1 - hh * s2) / (n1 * c1 + n2 * s2);
+    return q * q;
+}
+
+// handle_optics, src/tracer.jl:118-179.  Writes the evolved ray into `o`.
+__device__ __forceinline__ void handle_optics(const RayState& r, const HitDerivs& h, int32_t i, const Tri& T,
+                                              const splat_material_t& mat, float rndm, bool quirks,
+                                              RayState& o) {
+    const float Lc = r.lam, Xc = r.x, Yc = r.y;
+    const D Ld{r.lam, 1.0f}, Xd{r.x, 1.0f}, Yd{r.y, 1.0f};
+    // the reference differentiates the direction in y at y = r.x
+    const D Yq = quirks ? D{r.x, 1.0f} : Yd;
+
+    F3 N0 = N_at(r, h, T, Lc, Xc, Yc);
+    const bool in_med = r.medium != 0;
+    float n1c = in_med ? glass(mat, Lc) : air(Lc);
+    float n2c = in_med ? air(Lc) : glass(mat, Lc);
+    bool refracts = can_refract(r.dir, N0, n1c, n2c) && rndm > reflectance(r.dir, N0, n1c, n2c);
+
+    o.pos = next_p(r, h, Lc, Xc, Yc);
+    o.dpl = vpar(next_p(r, h, Ld, Xc, Yc));
+    o.dpx = vpar(next_p(r, h, Lc, Xd, Yc));
+    o.dpy = vpar(next_p(r, h, Lc, Xc, Yd));
+
+    if (refracts) {
+        o.dir = refract(r.dir, N0, n1c, n2c);
+        D n1d = in_med ? glass(mat, Ld) : air(Ld);
+        D n2d = in_med ? air(Ld) : glass(mat, Ld);
+        if (quirks) {
+            o.ddl = vpar(refract(d_expansion(r, Ld, Xc, Yc), N0, n1d, n2d));
+        } else {
+            o.ddl = vpar(refract(d_expansion(r, Ld, Xc, Yc), N_at(r, h, T, Ld, Xc, Yc), n1d, n2d));
+        }
+        o.ddx = vpar(refract(d_expansion(r, Lc, Xd, Yc), N_at(r, h, T, Lc, Xd, Yc), n1c, n2c));
+        o.ddy = vpar(refract(d_expansion(r, Lc, Xc, Yq), N_at(r, h, T, Lc, Xc, Yq), n1c, n2c));
+        o.medium = in_med ? 0 : 1;
+    } else {
+        o.dir = reflect(r.dir, N0);
+        o.ddl = vpar(reflect(d_expansion(r, Ld, Xc, Yc), N_at(r, h, T, Ld, Xc, Yc)));
+        o.ddx = vpar(reflect(d_expansion(r, Lc, Xd, Yc), N_at(r, h, T, Lc, Xd, Yc)));
+        o.ddy = vpar(reflect(d_expansion(r, Lc, Xc, Yq), N_at(r, h, T, Lc, Xc, Yq)));
+        o.medium = r.medium;
+    }
+    o.lam = r.lam;
+    o.x = r.x;
+    o.y = r.y;
+    o.ignore = i;
+}
+
+// final_evolution(r, i, t, ...), src/ray_imagers.jl:4-22: position moved onto
+// the hit with its partials; direction and its partials kept.
+__device__ __forceinline__ void final_evolution(const RayState& r, const HitDerivs& h, int32_t i, RayState& o) {
+    const float Lc = r.lam, Xc = r.x, Yc = r.y;
+    o = r;
+    o.pos = next_p(r, h, Lc, Xc, Yc);
+    o.dpl = vpar(next_p(r, h, D{r.lam, 1.0f}, Xc, Yc));
+    o.dpx = vpar(next_p(r, h, Lc, D{r.x, 1.0f}, Yc));
+    o.dpy = vpar(next_p(r, h, Lc, Xc, D{r.y, 1.0f}));
+    o.ignore = i;
+}
+
+// One sample of atomic_spectrum_kernel2 (src/ray_imagers.jl:78-113):
+// expand -> tex_uv -> texel -> cosine_shading.  False when uv is not finite.
+__device__ __forceinline__ bool splat_sample(const RayState& r, const Tri& T, float lam, float xs, float ys,
+                                             int64_t W, int64_t H, int64_t& off_ij, float& intensity) {
+    F3 pos = p_expansion(r, lam, xs, ys);
+    F3 dir = d_expansion(r, lam, xs, ys);
+    float bu, bv;
+    reverse_uv(pos, T, bu, bv);
+    float bw = (1.0f - bu) - bv;
+    float U = (T.ta.x * bu + T.tb.x * bv) + T.tc.x * bw;
+    float Vt = (T.ta.y * bu + T.tb.y * bv) + T.tc.y * bw;
+    if (isnan(U) || isnan(Vt) || isinf(U) || isinf(Vt)) return false;
+    float ci = ceilf(U * (float)W), cj = ceilf(Vt * (float)H);
+    ci = fminf(fmaxf(ci, 1.0f), (float)W);
+    cj = fminf(fmaxf(cj, 1.0f), (float)H);
+    off_ij = ((int64_t)ci - 1) + ((int64_t)cj - 1) * W;
+    F3 n = (T.na * bu + T.nb * bv) + T.nc * bw;
+    intensity = fabsf(dot(normalize(n), normalize(dir)));
+    return true;
+}
+
+}  // namespace splat

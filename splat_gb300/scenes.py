@@ -1,0 +1,328 @@
+"""Procedural scenes and the trace-step workloads.
+
+The reference ships only two usable meshes (objs/icos.obj, objs/smol_menger.obj)
+and builds its scenes in Julia scripts (src/scenes/*.jl).  The workloads here
+are seeded procedural stand-ins with the sizes the benchmarks are quoted on:
+
+* ``plain_small``   -- icosphere subdivision 5 (10,242 verts / 20,480 tris),
+  radius 1, over a 2-triangle diffuse floor at y = -1.5; one directional
+  RectLight, 256 x 256 rays, one uniform wavelength per ray, depth 3,
+  brute-force hitter, 256 x 256 Float32 light map.
+* ``realtime``      -- radially displaced icosphere subdivision 6 (40,962
+  verts / 81,920 tris, value-noise amplitude 0.05) over the floor; 2^20
+  traced rays (2048 x 2048 light grid, forward upscale 2 so every ray is
+  splatted at 2 x 2 footprint offsets through its position Jacobian), 16
+  stratified wavelengths, depth 4, BVH hitter, 1024 x 1024 x 16 int32
+  fixed-point light map (scale 2^16).
+* ``menger``        -- Menger sponge level 3 (8,000 cubes, 96,000 tris) of
+  glass rotated by a seeded quaternion inside a 12-triangle diffuse box;
+  2^22 rays, 8 wavelengths, depth 6, 2048 x 2048 x 8 map.
+
+Triangle arrays follow the reference layout: ``(T, 10, 3)`` float32 FTri
+records, index 0 (reference index 1) the all-zero sentinel, glass triangles
+first and diffuse triangles from ``first_diffuse`` (1-based) on, as the
+reference's scenes arrange them (src/scenes/sphere.jl:36-37).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field, replace
+from typing import Optional
+
+import numpy as np
+
+from . import types as T
+
+# --------------------------------------------------------------------------
+# meshes (float64 construction, float32 records)
+# --------------------------------------------------------------------------
+
+
+def _normalize(v: np.ndarray) -> np.ndarray:
+    return v / np.linalg.norm(v, axis=-1, keepdims=True)
+
+
+def icosphere(subdiv: int):
+    """Vertices (unit sphere) and CCW faces of a subdivided icosahedron."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    verts = np.array(
+        [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t),
+         (0, -1, -t), (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)],
+        dtype=np.float64,
+    )
+    faces = np.array(
+        [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+         (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+         (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)],
+        dtype=np.int64,
+    )
+    V = _normalize(verts)
+    F = faces
+    for _ in range(subdiv):
+        a, b, c = F[:, 0], F[:, 1], F[:, 2]
+        e = np.concatenate([np.stack([a, b], 1), np.stack([b, c], 1), np.stack([c, a], 1)], 0)
+        e = np.sort(e, axis=1)
+        uniq, inv = np.unique(e, axis=0, return_inverse=True)
+        inv = inv.reshape(-1)
+        mid = _normalize(0.5 * (V[uniq[:, 0]] + V[uniq[:, 1]]))
+        nf = F.shape[0]
+        mab, mbc, mca = (inv[:nf] + len(V), inv[nf:2 * nf] + len(V), inv[2 * nf:] + len(V))
+        V = np.concatenate([V, mid], 0)
+        F = np.concatenate(
+            [np.stack([a, mab, mca], 1), np.stack([b, mbc, mab], 1),
+             np.stack([c, mca, mbc], 1), np.stack([mab, mbc, mca], 1)], 0)
+    return V, F
+
+
+def value_noise(p: np.ndarray, freq: float, seed: int) -> np.ndarray:
+    """Seeded 3-D value noise in [-1, 1]: random lattice values, smoothstep
+    trilinear interpolation."""
+    rng = np.random.default_rng(seed)
+    n = 64
+    lattice = rng.uniform(-1.0, 1.0, size=(n, n, n))
+    q = p * freq + n / 2
+    i0 = np.floor(q).astype(np.int64)
+    f = q - i0
+    w = f * f * (3.0 - 2.0 * f)
+    out = np.zeros(p.shape[0])
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                wt = ((w[:, 0] if dx else 1 - w[:, 0]) * (w[:, 1] if dy else 1 - w[:, 1])
+                      * (w[:, 2] if dz else 1 - w[:, 2]))
+                out += wt * lattice[(i0[:, 0] + dx) % n, (i0[:, 1] + dy) % n, (i0[:, 2] + dz) % n]
+    return out
+
+
+def vertex_normals(V: np.ndarray, F: np.ndarray) -> np.ndarray:
+    fn = np.cross(V[F[:, 1]] - V[F[:, 0]], V[F[:, 2]] - V[F[:, 0]])
+    acc = np.zeros_like(V)
+    for k in range(3):
+        np.add.at(acc, F[:, k], fn)
+    return _normalize(acc)
+
+
+def ftri_records(P: np.ndarray, N: np.ndarray, UV: np.ndarray) -> np.ndarray:
+    """Pack per-corner positions / normals / uvs ``(T, 3, 3)`` into FTri
+    records.  The plane normal is ``cross(v1 - v2, v2 - v3)`` in binary32, as
+    mesh_to_FTri computes it (src/geo.jl:331-341)."""
+    P = P.astype(np.float32)
+    v1, v2, v3 = P[:, 0], P[:, 1], P[:, 2]
+    a = v1 - v2
+    b = v2 - v3
+    n = np.stack([a[:, 1] * b[:, 2] - a[:, 2] * b[:, 1],
+                  a[:, 2] * b[:, 0] - a[:, 0] * b[:, 2],
+                  a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0]], 1).astype(np.float32)
+    out = np.zeros((P.shape[0], 10, 3), dtype=np.float32)
+    out[:, 0] = n
+    out[:, 1:4] = P
+    out[:, 4:7] = N.astype(np.float32)
+    out[:, 7:10] = UV.astype(np.float32)
+    return out
+
+
+def sphere_tris(subdiv: int, radius: float = 1.0, noise_amp: float = 0.0, noise_seed: int = 3,
+                center=(0.0, 0.0, 0.0)) -> np.ndarray:
+    V, F = icosphere(subdiv)
+    if noise_amp:
+        V = V * (1.0 + noise_amp * value_noise(V, 3.0, noise_seed))[:, None]
+    V = V * radius + np.asarray(center, dtype=np.float64)
+    N = vertex_normals(V, F) if noise_amp else _normalize(V - np.asarray(center))
+    P = V[F]
+    NN = N[F]
+    UV = np.zeros_like(P)
+    return ftri_records(P, NN, UV)
+
+
+def floor_tris(y: float = -1.5, half: float = 4.0) -> np.ndarray:
+    c = np.array([[-half, y, -half], [half, y, -half], [half, y, half], [-half, y, half]])
+    P = np.stack([c[[0, 2, 1]], c[[0, 3, 2]]], 0)
+    N = np.zeros_like(P)
+    N[..., 1] = 1.0
+    UV = np.zeros_like(P)
+    UV[..., 0] = (P[..., 0] + half) / (2 * half)
+    UV[..., 1] = (P[..., 2] + half) / (2 * half)
+    return ftri_records(P, N, UV)
+
+
+_CUBE_FACES = [  # (normal axis, sign) -> 4 corners (unit cube) CCW seen from outside
+    ((0, 0, -1), [(0, 0, 0), (0, 1, 0), (1, 1, 0), (1, 0, 0)]),
+    ((0, 0, 1), [(0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]),
+    ((0, -1, 0), [(0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1)]),
+    ((0, 1, 0), [(0, 1, 0), (0, 1, 1), (1, 1, 1), (1, 1, 0)]),
+    ((-1, 0, 0), [(0, 0, 0), (0, 0, 1), (0, 1, 1), (0, 1, 0)]),
+    ((1, 0, 0), [(1, 0, 0), (1, 1, 0), (1, 1, 1), (1, 0, 1)]),
+]
+
+
+def _cube_corner_tris():
+    P, N = [], []
+    for n, q in _CUBE_FACES:
+        q = np.asarray(q, dtype=np.float64)
+        P += [q[[0, 1, 2]], q[[0, 2, 3]]]
+        N += [np.tile(n, (3, 1))] * 2
+    return np.asarray(P), np.asarray(N, dtype=np.float64)
+
+
+def menger_cubes(level: int) -> np.ndarray:
+    n = 3 ** level
+    idx = np.stack(np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij"), -1).reshape(-1, 3)
+    keep = np.ones(len(idx), dtype=bool)
+    d = idx.copy()
+    for _ in range(level):
+        ones = (d % 3 == 1).sum(1)
+        keep &= ones < 2
+        d //= 3
+    return idx[keep]
+
+
+def random_quaternion_matrix(seed: int) -> np.ndarray:
+    """Uniform random rotation (Shoemake's subgroup algorithm)."""
+    u1, u2, u3 = np.random.default_rng(seed).uniform(size=3)
+    q = np.array([np.sqrt(1 - u1) * np.sin(2 * np.pi * u2), np.sqrt(1 - u1) * np.cos(2 * np.pi * u2),
+                  np.sqrt(u1) * np.sin(2 * np.pi * u3), np.sqrt(u1) * np.cos(2 * np.pi * u3)])
+    x, y, z, w = q
+    return np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                     [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                     [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+
+
+def menger_tris(level: int, size: float = 2.0, rotation_seed: Optional[int] = 4) -> np.ndarray:
+    cubes = menger_cubes(level)
+    s = size / 3 ** level
+    Pc, Nc = _cube_corner_tris()
+    P = (-size / 2 + (cubes[:, None, None, :] + Pc[None]) * s).reshape(-1, 3, 3)
+    N = np.broadcast_to(Nc[None], (len(cubes),) + Nc.shape).reshape(-1, 3, 3)
+    if rotation_seed is not None:
+        R = random_quaternion_matrix(rotation_seed)
+        P = P @ R.T
+        N = N @ R.T
+    return ftri_records(P, N, np.zeros_like(P))
+
+
+def box_tris(half: float = 3.0) -> np.ndarray:
+    """12 inward-facing triangles; texture atlas of 3 x 2 face cells."""
+    Pc, Nc = _cube_corner_tris()
+    P = (Pc - 0.5) * 2 * half
+    N = -Nc
+    UV = np.zeros_like(P)
+    for f in range(6):
+        axis = int(np.nonzero(Nc[2 * f, 0])[0][0])
+        a1, a2 = [k for k in range(3) if k != axis]
+        cx, cy = f % 3, f // 3
+        for t in (2 * f, 2 * f + 1):
+            loc = Pc[t]
+            UV[t, :, 0] = (cx + loc[:, a1]) / 3.0
+            UV[t, :, 1] = (cy + loc[:, a2]) / 2.0
+    P = P[:, ::-1]  # reverse winding: normals point into the box
+    N = N[:, ::-1]
+    UV = UV[:, ::-1]
+    return ftri_records(P, N, UV)
+
+
+def assemble(glass: np.ndarray, diffuse: np.ndarray):
+    """Sentinel + glass + diffuse; returns (tris, first_diffuse 1-based)."""
+    sentinel = np.zeros((1, 10, 3), dtype=np.float32)
+    tris = np.concatenate([sentinel, glass, diffuse], 0).astype(np.float32)
+    return np.ascontiguousarray(tris), 1 + glass.shape[0] + 1
+
+
+# --------------------------------------------------------------------------
+# lights and workloads
+# --------------------------------------------------------------------------
+
+
+def hemisphere_light(seed: int, res: int, aperture: float, distance: float = 3.0, min_elev: float = 0.5):
+    rng = np.random.default_rng(seed)
+    y = rng.uniform(min_elev, 1.0)
+    phi = rng.uniform(0.0, 2 * np.pi)
+    u = np.array([np.sqrt(1 - y * y) * np.cos(phi), y, np.sqrt(1 - y * y) * np.sin(phi)])
+    e = np.array([0.0, 0.0, 1.0]) if abs(u[2]) < 0.9 else np.array([1.0, 0.0, 0.0])
+    d1 = _normalize(np.cross(u, e))
+    d2 = np.cross(u, d1)
+    return T.rect_light(distance * u, -u, aperture * d1, aperture * d2, res, res)
+
+
+@dataclass
+class Workload:
+    name: str
+    tris: np.ndarray
+    first_diffuse: int
+    light: np.ndarray
+    upscale: int = 1
+    lambda_mode: tuple = (T.LAMBDA_FIXED, 1, 550.0, 550.0)  # (mode, n_strata, l0, l1)
+    spectrum: Optional[np.ndarray] = None  # None: each ray splats at its own wavelength
+    depth: int = 3
+    material: tuple = (T.MATERIAL_LINEAR_REF, 0.0, 0.0)
+    map_w: int = 256
+    map_h: int = 256
+    accum: str = "f32"  # "f32" float atomics or "i32" fixed point
+    frac_bits: int = 16
+    hitter: str = "brute"
+    seed: int = 2
+    force_rand: Optional[float] = None
+    quirks: bool = True
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def n_rays(self) -> int:
+        return int(self.light["res1"] // self.upscale) * int(self.light["res2"] // self.upscale)
+
+    @property
+    def n_planes(self) -> int:
+        return 1 if self.spectrum is None else int(len(self.spectrum))
+
+    @property
+    def n_tris(self) -> int:
+        return int(self.tris.shape[0])
+
+    def with_(self, **kw) -> "Workload":
+        return replace(self, **kw)
+
+
+CAUCHY_GLASS = (T.MATERIAL_CAUCHY, 1.5, 0.004)
+
+
+def stratified_spectrum(n: int, lo: float = 400.0, hi: float = 700.0) -> np.ndarray:
+    w = np.float32((hi - lo) / n)
+    return (np.float32(lo) + (np.arange(n, dtype=np.float32) + np.float32(0.5)) * w).astype(np.float32)
+
+
+def plain_small(**kw) -> Workload:
+    tris, fd = assemble(sphere_tris(5), floor_tris(-1.5, 4.0))
+    w = Workload(
+        name="icosphere5-20480tris-65536rays-depth3-brute-256x256-f32",
+        tris=tris, first_diffuse=fd, light=hemisphere_light(1, 256, 1.05), upscale=1,
+        lambda_mode=(T.LAMBDA_UNIFORM, 1, 400.0, 700.0), spectrum=None, depth=3,
+        material=CAUCHY_GLASS, map_w=256, map_h=256, accum="f32", hitter="brute", seed=2,
+    )
+    return w.with_(**kw) if kw else w
+
+
+def realtime(**kw) -> Workload:
+    tris, fd = assemble(sphere_tris(6, noise_amp=0.05, noise_seed=3), floor_tris(-1.5, 4.0))
+    w = Workload(
+        name="displaced-icosphere6-81920tris-2^20rays-16lambda-depth4-bvh-1024x1024-i32",
+        tris=tris, first_diffuse=fd, light=hemisphere_light(1, 2048, 1.1), upscale=2,
+        lambda_mode=(T.LAMBDA_STRATIFIED, 16, 400.0, 700.0), spectrum=stratified_spectrum(16), depth=4,
+        material=CAUCHY_GLASS, map_w=1024, map_h=1024, accum="i32", hitter="bvh", seed=2,
+    )
+    return w.with_(**kw) if kw else w
+
+
+def menger(**kw) -> Workload:
+    tris, fd = assemble(menger_tris(3, 2.0, 4), box_tris(3.0))
+    light = T.rect_light((0.0, 2.6, 0.0), (0.0, -1.0, 0.0), (1.3, 0.0, 0.0), (0.0, 0.0, 1.3), 2048, 2048)
+    w = Workload(
+        name="menger3-96000tris-box-2^22rays-8lambda-depth6-bvh-2048x2048-i32",
+        tris=tris, first_diffuse=fd, light=light, upscale=1,
+        lambda_mode=(T.LAMBDA_STRATIFIED, 8, 400.0, 700.0), spectrum=stratified_spectrum(8), depth=6,
+        material=CAUCHY_GLASS, map_w=2048, map_h=2048, accum="i32", hitter="bvh", seed=2,
+    )
+    return w.with_(**kw) if kw else w
+
+
+def scaled_light(light: np.ndarray, res: int) -> np.ndarray:
+    out = light.copy()
+    out["res1"] = res
+    out["res2"] = res
+    return out

@@ -1,0 +1,61 @@
+"""Shared test inputs and comparisons."""
+from __future__ import annotations
+
+import numpy as np
+
+from splat_gb300 import scenes as S
+from splat_gb300 import types as T
+
+FLOAT_FIELDS = ["pos", "dp_dl", "dp_dx", "dp_dy", "dir", "dd_dl", "dd_dx", "dd_dy", "lam", "x", "y"]
+
+
+def small_scene(subdiv: int = 2, noise: float = 0.0):
+    return S.assemble(S.sphere_tris(subdiv, noise_amp=noise), S.floor_tris(-1.5, 4.0))
+
+
+def random_rays(n: int, seed: int, n_tris: int, aim: float = 0.7) -> np.ndarray:
+    """Rays around a unit sphere: a fraction aimed at it, the rest random;
+    random ignore_tri values (some real triangle indices)."""
+    rng = np.random.default_rng(seed)
+    rays = np.zeros(n, dtype=T.ADRAY)
+    o = rng.normal(size=(n, 3))
+    o = 3.0 * o / np.linalg.norm(o, axis=1, keepdims=True)
+    d = rng.normal(size=(n, 3))
+    aimed = rng.uniform(size=n) < aim
+    tgt = rng.uniform(-0.8, 0.8, size=(n, 3))
+    d[aimed] = tgt[aimed] - o[aimed]
+    d = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays["pos"] = o.astype(np.float32)
+    rays["dir"] = d.astype(np.float32)
+    rays["dp_dx"] = rng.normal(scale=0.01, size=(n, 3)).astype(np.float32)
+    rays["dp_dy"] = rng.normal(scale=0.01, size=(n, 3)).astype(np.float32)
+    rays["lam"] = rng.uniform(400, 700, size=n).astype(np.float32)
+    rays["x"] = rng.uniform(1, 64, size=n).astype(np.float32)
+    rays["y"] = rng.uniform(1, 64, size=n).astype(np.float32)
+    rays["ignore_tri"] = np.where(rng.uniform(size=n) < 0.3, rng.integers(1, n_tris + 1, size=n), 1)
+    rays["status"] = T.STATUS_ACTIVE
+    return rays
+
+
+def float_equal(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Elementwise numeric equality with NaN == NaN (signed zeros equal)."""
+    return (a == b) | (np.isnan(a) & np.isnan(b))
+
+
+def assert_rays_equal(got: np.ndarray, ref: np.ndarray, what: str = "rays"):
+    assert got.shape == ref.shape
+    for f in ["status", "ignore_tri", "in_medium", "dest"]:
+        bad = got[f] != ref[f]
+        assert not bad.any(), f"{what}: field {f} differs at {np.nonzero(bad)[0][:10]}"
+    for f in FLOAT_FIELDS:
+        eq = float_equal(got[f], ref[f])
+        if eq.ndim > 1:
+            eq = eq.all(axis=1)
+        assert eq.all(), (f"{what}: field {f} differs at {np.nonzero(~eq)[0][:10]}: "
+                          f"{got[f][~eq][:3]} vs {ref[f][~eq][:3]}")
+
+
+def rel_l1(a: np.ndarray, b: np.ndarray) -> float:
+    a = a.astype(np.float64)
+    b = b.astype(np.float64)
+    return float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))

@@ -1,0 +1,96 @@
+"""The C ABI without a GPU: libsplat.so loads, exports every function
+include/splat.h declares, and the ctypes records match the header's layout
+(checked by compiling a C program against the header)."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from splat_gb300 import _lib as L
+from splat_gb300 import types as T
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "splat.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(splat_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = L.load()
+    declared = header_functions()
+    assert len(declared) >= 15
+    missing = [f for f in declared if not hasattr(lib, f)]
+    assert not missing, f"not exported: {missing}"
+    assert set(declared) == set(L.SIGNATURES), "ctypes signatures out of sync with the header"
+    assert lib.splat_abi_version() == 1
+
+
+LAYOUT_C = r"""
+#include <stddef.h>
+#include <stdio.h>
+#include "splat.h"
+#define P(T) printf(#T " %zu\n", sizeof(T));
+#define O(T, f) printf(#T "." #f " %zu\n", offsetof(T, f));
+int main(void) {
+  P(splat_adray_t) P(splat_ftri_t) P(splat_ntri_t) P(splat_rect_light_t) P(splat_material_t)
+  P(splat_lambda_mode_t) P(splat_trace_params_t) P(splat_trace_stats_t) P(splat_scene_info_t)
+  O(splat_adray_t, in_medium) O(splat_adray_t, ignore_tri) O(splat_adray_t, dest) O(splat_adray_t, lambda)
+  O(splat_adray_t, status)
+  O(splat_trace_params_t, upscale) O(splat_trace_params_t, seed) O(splat_trace_params_t, material)
+  O(splat_trace_params_t, force_rand) O(splat_trace_params_t, spectrum) O(splat_trace_params_t, map_w)
+  O(splat_trace_params_t, accum) O(splat_trace_params_t, ray_begin) O(splat_trace_params_t, ray_end)
+  O(splat_scene_info_t, device_bytes) O(splat_scene_info_t, bvh_pad)
+  return 0;
+}
+"""
+
+
+def c_layout():
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "layout.c")
+        exe = os.path.join(d, "layout")
+        open(src, "w").write(LAYOUT_C)
+        subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
+        out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    return {k: int(v) for k, v in (line.split() for line in out.strip().splitlines())}
+
+
+def test_record_layouts_match_header():
+    c = c_layout()
+    # Julia isbits layouts of the reference (src/geo.jl:60-76, :18; src/ray_generators.jl:4-11)
+    assert c["splat_adray_t"] == 136 == T.ADRAY.itemsize
+    assert c["splat_adray_t.ignore_tri"] == 104 and c["splat_adray_t.dest"] == 112
+    assert c["splat_adray_t.lambda"] == 120 and c["splat_adray_t.status"] == 132
+    assert c["splat_ftri_t"] == T.FTRI_BYTES
+    assert c["splat_ntri_t"] == 52
+    assert c["splat_rect_light_t"] == 64 == T.RECT_LIGHT.itemsize
+    for name, cls in [("splat_trace_params_t", L.TraceParams), ("splat_trace_stats_t", L.TraceStats),
+                      ("splat_scene_info_t", L.SceneInfo), ("splat_material_t", L.Material),
+                      ("splat_lambda_mode_t", L.LambdaMode), ("splat_rect_light_t", L.RectLight)]:
+        assert c[name] == C.sizeof(cls), name
+    for f in ["upscale", "seed", "material", "force_rand", "spectrum", "map_w", "accum", "ray_begin", "ray_end"]:
+        assert c[f"splat_trace_params_t.{f}"] == getattr(L.TraceParams, f).offset, f
+    assert c["splat_scene_info_t.bvh_pad"] == L.SceneInfo.bvh_pad.offset
+    for f, off in [("in_medium", 96), ("ignore_tri", 104), ("dest", 112), ("lam", 120), ("status", 132)]:
+        assert T.ADRAY.fields[f][1] == off
+
+
+def test_invalid_arguments_fail_cleanly_without_gpu():
+    """Argument validation happens before any CUDA call."""
+    lib = L.load()
+    P = L.TraceParams()
+    rc = lib.splat_trace_forward(None, C.byref(P), None, None, 0, None, None)
+    assert rc == L.ERR_INVALID
+    assert b"null" in lib.splat_last_error()
+    rc = lib.splat_scene_create(None, 0, 2, 0, None, None)
+    assert rc == L.ERR_INVALID
+    assert lib.splat_trace_workspace_size(1000) > 1000 * 117 * 2
+    with pytest.raises(L.SplatError):
+        L.check(L.ERR_INVALID)

@@ -1,0 +1,125 @@
+"""The fused forward trace step (splat_trace_forward) against the CPU
+restatement of the forward half of trace! (src/tracer.jl:317-342).
+
+Small and sampled cases compare whole light maps with the oracle
+(fixed-point maps bit-exact, float maps within 1e-5 relative L1).  At the
+benchmark sizes, size-independent properties: brute force == BVH, run-to-run
+identity of fixed-point maps, and linearity (the map of all rays equals the
+sum of the maps of disjoint ray ranges), plus oracle checks of sampled ranges."""
+import numpy as np
+import pytest
+
+from helpers import rel_l1
+from oracle import oracle as O
+from splat_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _gpu(wl, ray_begin=0, ray_end=0, scene=None):
+    from splat_gb300 import tracer
+
+    r = tracer.trace_forward(wl, scene=scene, ray_begin=ray_begin, ray_end=ray_end)
+    return r.tex.cpu().numpy().ravel(), r.stats
+
+
+def _cmp(wl, got, ref_tex):
+    ref = ref_tex.ravel(order="F")
+    if wl.accum == "i32":
+        bad = np.nonzero(got != ref)[0]
+        assert bad.size == 0, f"{bad.size} texels differ, first {bad[:8]}: {got[bad[:8]]} vs {ref[bad[:8]]}"
+    else:
+        assert rel_l1(got, ref) <= 1e-5
+
+
+@pytest.mark.parametrize("accum", ["f32", "i32"])
+@pytest.mark.parametrize("hitter", ["brute", "bvh"])
+def test_plain_small_reduced(torch_cuda, accum, hitter):
+    wl = S.plain_small(light=S.scaled_light(S.plain_small().light, 96), accum=accum, hitter=hitter)
+    got, st = _gpu(wl)
+    ref_tex, ref_st, _ = O.trace_forward(wl)
+    assert st["rays_per_bounce"] == [int(x) for x in ref_st[: wl.depth]]
+    assert st["diffuse"] == int(ref_st[6]) and st["samples"] == int(ref_st[7])
+    _cmp(wl, got, ref_tex)
+
+
+@pytest.mark.parametrize("force_rand,quirks", [(0.0, True), (1.0, True), (None, False)])
+def test_plain_small_variants(torch_cuda, force_rand, quirks):
+    wl = S.plain_small(light=S.scaled_light(S.plain_small().light, 64), accum="i32", force_rand=force_rand,
+                       quirks=quirks, material=(0, 0.0, 0.0))
+    got, st = _gpu(wl)
+    ref_tex, ref_st, _ = O.trace_forward(wl)
+    assert st["rays_per_bounce"] == [int(x) for x in ref_st[: wl.depth]]
+    _cmp(wl, got, ref_tex)
+
+
+def test_plain_small_full_size(torch_cuda):
+    """The 2^16-ray, 20,480-triangle brute-force workload at full size."""
+    wl = S.plain_small()
+    got, st = _gpu(wl)
+    ref_tex, ref_st, _ = O.trace_forward(wl)
+    assert st["rays_per_bounce"] == [int(x) for x in ref_st[: wl.depth]]
+    _cmp(wl, got, ref_tex)
+    wl_i = wl.with_(accum="i32")
+    got_i, _ = _gpu(wl_i)
+    ref_i, _, _ = O.trace_forward(wl_i)
+    _cmp(wl_i, got_i, ref_i)
+
+
+@pytest.mark.parametrize("make", [S.realtime, S.menger], ids=["realtime", "menger"])
+def test_sampled_ranges_match_oracle(torch_cuda, make):
+    """Full-size workloads, disjoint ray ranges in the middle of the light
+    grid traced alone, each compared with the oracle."""
+    from splat_gb300 import tracer
+
+    wl = make()
+    scene = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
+    n = wl.n_rays
+    h = int(wl.light["res1"]) // wl.upscale
+    for c in (n // 2 + h // 2 - 600, n // 3 + h // 3):
+        got, st = _gpu(wl, c, c + 1200, scene=scene)
+        ref_tex, ref_st, _ = O.trace_forward(wl, c, c + 1200)
+        assert st["rays_per_bounce"] == [int(x) for x in ref_st[: wl.depth]]
+        assert ref_st[1] > 0, "the sample should reach the glass"
+        _cmp(wl, got, ref_tex)
+
+
+def test_realtime_full_size_properties(torch_cuda):
+    """2^20 rays / 81,922 triangles: BVH == brute force, run-to-run identity,
+    and linearity over disjoint ray ranges (int32 accumulation)."""
+    from splat_gb300 import tracer
+
+    wl = S.realtime()
+    scene = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
+    a, sa = _gpu(wl, scene=scene)
+    b, sb = _gpu(wl, scene=scene)
+    assert np.array_equal(a, b) and sa == sb
+    c, sc = _gpu(wl.with_(hitter="brute"), scene=scene)
+    assert np.array_equal(a, c) and sa["rays_per_bounce"] == sc["rays_per_bounce"]
+    n = wl.n_rays
+    cuts = [0, n // 3, n // 2 + 17, n]
+    parts = sum(_gpu(wl, lo, hi, scene=scene)[0].astype(np.int64) for lo, hi in zip(cuts[:-1], cuts[1:]))
+    assert np.array_equal(parts, a.astype(np.int64))
+    assert sa["diffuse"] > n // 2 and a.sum() > 0
+
+
+def test_host_entry_point_matches_device(torch_cuda):
+    """splat_trace_forward_host (host triangles in, host map out, scene
+    repack + BVH refit in between) equals the resident-scene step."""
+    from splat_gb300 import tracer
+
+    wl = S.realtime(light=S.scaled_light(S.realtime().light, 512))
+    step = tracer.TraceStep(wl)
+    dev = step.run().cpu().numpy().ravel()
+    host_map = np.zeros(dev.shape, dtype=np.int32)
+    st = step.run_host(np.ascontiguousarray(wl.tris), host_map)
+    assert np.array_equal(host_map, dev)
+    assert st["rays_per_bounce"] == step.stats()["rays_per_bounce"]
