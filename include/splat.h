@@ -255,7 +255,8 @@ enum {
     SPLAT_KERNEL_HIT_BVH = 2,
     SPLAT_KERNEL_EVOLVE = 3,
     SPLAT_KERNEL_AUX = 4, /* fills, unpacks, conversions, stats, refit, packing */
-    SPLAT_KERNEL_KINDS = 5
+    SPLAT_KERNEL_SPLAT = 5,
+    SPLAT_KERNEL_KINDS = 6
 };
 typedef struct splat_profile splat_profile_t;
 splat_status_t splat_profile_create(int32_t max_launches, splat_profile_t** out);

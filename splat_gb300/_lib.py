@@ -103,7 +103,8 @@ KERNEL_HIT_BRUTE = 1
 KERNEL_HIT_BVH = 2
 KERNEL_EVOLVE = 3
 KERNEL_AUX = 4
-KERNEL_ALL = 5
+KERNEL_SPLAT = 5
+KERNEL_ALL = 6
 
 _lib = None
 _lock = threading.Lock()

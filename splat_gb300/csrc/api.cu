@@ -69,15 +69,16 @@ RaySoA carve_soa(char*& p, int64_t cap) {
 // Bounce-loop scratch: two SoA ray buffers, hit indices, the packed-argmin
 // array of split brute-force launches, counters and the kernel error word.
 struct Work {
-    RaySoA a, b;
+    RaySoA a, b, q;  // bounce ping-pong buffers and the splat queue
     int32_t* hit;
     uint64_t* tmp;
-    int64_t* counts;  // counts[b] = active rays after bounce b (b <= 64)
+    int64_t* counts;  // counts[b] = active rays after bounce b (b <= 64); counts[kSplatCount] = queued
 };
+constexpr int kSplatCount = 96;
 constexpr size_t kCounterBytes = 1024;
 
 size_t work_bytes(int64_t cap) {
-    return 2 * soa_bytes(cap) + align_up(4 * (size_t)cap) + align_up(8 * (size_t)cap) + kCounterBytes + kAlign;
+    return 3 * soa_bytes(cap) + align_up(4 * (size_t)cap) + align_up(8 * (size_t)cap) + kCounterBytes + kAlign;
 }
 
 Work carve_work(void* ws, int64_t cap) {
@@ -85,6 +86,7 @@ Work carve_work(void* ws, int64_t cap) {
     Work w;
     w.a = carve_soa(p, cap);
     w.b = carve_soa(p, cap);
+    w.q = carve_soa(p, cap);
     w.hit = reinterpret_cast<int32_t*>(p);
     p += align_up(4 * (size_t)cap);
     w.tmp = reinterpret_cast<uint64_t*>(p);
@@ -560,8 +562,10 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
     ea.seed = P->seed;
     ea.force_rand = P->force_rand;
     ea.quirks = (P->flags & SPLAT_FLAG_REF_QUIRKS) ? 1 : 0;
-    ea.sp = make_splat(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
-    ea.stats = d_stats;
+    const SplatParams sp =
+        make_splat(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
+    ea.splat_q = w.q;
+    ea.splat_count = &w.counts[kSplatCount];
     RaySoA cur = w.a, nxt = w.b;
     for (int32_t b = 1; b <= P->depth; ++b) {
         RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0};
@@ -580,9 +584,14 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
         }
         std::swap(cur, nxt);
     }
+    {
+        ProfScope ps(SPLAT_KERNEL_SPLAT, st);
+        SPLAT_CUDA(launch_splat(w.q, &w.counts[kSplatCount], scene->d_ftri, sp, d_stats, sm, st), "splat");
+    }
     if (d_stats) {
         ProfScope ps(SPLAT_KERNEL_AUX, st);
-        SPLAT_CUDA(launch_stats_finish(w.counts, P->depth, d_stats, scene->d_err, st), "stats");
+        SPLAT_CUDA(launch_stats_finish(w.counts, P->depth, &w.counts[kSplatCount], d_stats, scene->d_err, st),
+                   "stats");
     }
     return SPLAT_OK;
 }

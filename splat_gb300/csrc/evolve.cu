@@ -1,8 +1,8 @@
 // evolve.cu -- evolve_ray over the active rays of one bounce, with the ray
-// compaction (warp ballot + block scan, one atomic per block) fused in, and
-// in trace mode the diffuse rays' final_evolution + light-map splat fused in
-// as well, so a diffuse ray is splatted in the bounce that finds it and never
-// stored.
+// compaction (warp ballot + block scan, one atomic per block) fused in.  In
+// trace mode the diffuse rays' final_evolution is fused in as well and the
+// result is compacted into a splat queue; one splat launch per frame then
+// spreads (ray, sample) pairs over full warps.
 //
 // Reference: evolve_ray src/tracer.jl:181-201, partition! src/partition.jl
 // (semantics: the active rays, in any order, and their count),
@@ -10,9 +10,9 @@
 // src/ray_imagers.jl:78-113.  Each ray's Fresnel draw is keyed by its id, so
 // results do not depend on the order compaction leaves the rays in.
 //
-// Splat: a warp takes its diffuse rays one at a time (state broadcast by
-// shuffles) and spreads that ray's n_lambda x N x N samples over its lanes.
-// Fixed-point maps add round(intensity * 2^frac_bits) with warp-aggregated
+// Splat: one thread per (queued ray, sample); a ray's n_lambda x N x N
+// samples are consecutive, so a warp's lanes share (broadcast-load) one or a
+// few rays.  Fixed-point maps add round(intensity * 2^frac_bits) with warp-aggregated
 // integer atomics (lanes on the same texel are summed by match_any +
 // reduce_add first), which makes the map independent of ray order and
 // bit-exact run to run.  Float maps use plain float atomics, as the
@@ -140,7 +140,8 @@ __device__ __forceinline__ void add_stats(splat_trace_stats_t* st, int diffuse, 
 template <bool TRACE>
 __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
     __shared__ int s_warp[kEvolveThreads / 32];
-    __shared__ unsigned long long s_base;
+    __shared__ int s_wdif[kEvolveThreads / 32];
+    __shared__ unsigned long long s_base, s_dbase;
     const int64_t n = *A.in_count;
     const int lane = lane_id();
     const int wid = threadIdx.x >> 5;
@@ -174,27 +175,34 @@ __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
                 keep = true;
             }
         }
-        // compaction: ballot -> block scan -> one atomic per block
+        // compaction of the survivors (and, tracing, of the diffuse rays into
+        // the splat queue): ballot -> block scan -> one atomic per block each
         const unsigned kb = __ballot_sync(kFull, keep);
-        if (lane == 0) s_warp[wid] = __popc(kb);
+        const unsigned db = TRACE ? __ballot_sync(kFull, dif) : 0u;
+        if (lane == 0) {
+            s_warp[wid] = __popc(kb);
+            s_wdif[wid] = __popc(db);
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
-            int tot = 0;
+            int tot = 0, dtot = 0;
             for (int w = 0; w < kEvolveThreads / 32; ++w) {
-                const int c = s_warp[w];
+                const int c = s_warp[w], d = s_wdif[w];
                 s_warp[w] = tot;
+                s_wdif[w] = dtot;
                 tot += c;
+                dtot += d;
             }
             s_base = tot ? atomicAdd(reinterpret_cast<unsigned long long*>(A.out_count), (unsigned long long)tot) : 0ull;
+            s_dbase = dtot ? atomicAdd(reinterpret_cast<unsigned long long*>(A.splat_count), (unsigned long long)dtot)
+                           : 0ull;
         }
         __syncthreads();
+        const unsigned below = (1u << lane) - 1u;
         if (keep) {
-            const int64_t pos = (int64_t)s_base + s_warp[wid] + __popc(kb & ((1u << lane) - 1u));
-            store_ray(A.out, pos, o, id);
-        }
-        if (TRACE) {
-            const int samples = splat_warp(A.sp, A.tris, dif, o, ih);
-            add_stats(A.stats, dif ? 1 : 0, samples);
+            store_ray(A.out, (int64_t)s_base + s_warp[wid] + __popc(kb & below), o, id);
+        } else if (TRACE && dif) {
+            store_ray(A.splat_q, (int64_t)s_dbase + s_wdif[wid] + __popc(db & below), o, id);
         }
         __syncthreads();
     }
@@ -258,16 +266,59 @@ cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_
     return cudaGetLastError();
 }
 
-__global__ void stats_finish_kernel(const int64_t* counts, int depth, splat_trace_stats_t* st, const int32_t* err) {
+// One thread per (queued diffuse ray, sample); loops over warp-sized chunks
+// so every lane of a warp reaches the aggregated atomics together.
+__global__ void __launch_bounds__(256) splat_kernel(RaySoA q, const int64_t* __restrict__ d_count,
+                                                    const splat_ftri_t* __restrict__ tris, SplatParams sp,
+                                                    splat_trace_stats_t* st) {
+    const int64_t n = *d_count;
+    const int S = (sp.n_lambda > 0 ? sp.n_lambda : 1) * sp.n_delta * sp.n_delta;
+    const int64_t total = n * S;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    int done = 0;
+    for (int64_t base = warp * 32; base < total; base += n_warps * 32) {
+        const int64_t g = base + lane_id();
+        bool ok = false;
+        int64_t off = 0;
+        float inten = 0.f;
+        if (g < total) {
+            const int64_t k = g / S;
+            const int s = (int)(g - k * S);
+            const RayState r = load_ray(q, k);
+            const Tri T = load_tri(tris, r.ignore);
+            ok = sample_of(sp, r, T, s, off, inten);
+        }
+        accumulate_warp(sp, ok, off, inten);
+        done += ok ? 1 : 0;
+    }
+    add_stats(st, 0, done);
+}
+
+cudaError_t launch_splat(const RaySoA& q, const int64_t* d_count, const splat_ftri_t* tris, const SplatParams& sp,
+                         splat_trace_stats_t* stats, int sm_count, cudaStream_t s) {
+    if (q.cap <= 0) return cudaSuccess;
+    const int S = (sp.n_lambda > 0 ? sp.n_lambda : 1) * sp.n_delta * sp.n_delta;
+    int64_t b = (q.cap * S + 255) / 256;
+    const int64_t lim = (int64_t)sm_count * 8;
+    if (b > lim) b = lim;
+    splat_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_count, tris, sp, stats);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+__global__ void stats_finish_kernel(const int64_t* counts, int depth, const int64_t* splat_count,
+                                    splat_trace_stats_t* st, const int32_t* err) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         for (int b = 0; b < 8; ++b) st->rays_per_bounce[b] = b < depth ? counts[b] : 0;
+        st->diffuse = splat_count ? *splat_count : st->diffuse;
         st->error = err ? *err : 0;
     }
 }
 
-cudaError_t launch_stats_finish(const int64_t* counts, int depth, splat_trace_stats_t* stats, const int32_t* err,
-                                cudaStream_t s) {
-    stats_finish_kernel<<<1, 32, 0, s>>>(counts, depth, stats, err);
+cudaError_t launch_stats_finish(const int64_t* counts, int depth, const int64_t* splat_count,
+                                splat_trace_stats_t* stats, const int32_t* err, cudaStream_t s) {
+    stats_finish_kernel<<<1, 32, 0, s>>>(counts, depth, splat_count, stats, err);
     ++g_launches;
     return cudaGetLastError();
 }

@@ -98,15 +98,18 @@ struct EvolveArgs {
     int32_t quirks;
     int32_t last;           // trace mode: last bounce, no optics
     splat_adray_t* aos;     // plugin mode: retired rays written back here
-    SplatParams sp;
-    splat_trace_stats_t* stats;
+    RaySoA splat_q;         // trace mode: final-evolved diffuse rays (ignore = hit triangle)
+    int64_t* splat_count;
 };
 cudaError_t launch_evolve_trace(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s);
 cudaError_t launch_evolve_plugin(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s);
 cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_idx, const splat_ftri_t* tris,
                              int64_t n_tris, int32_t* err, const SplatParams& sp, int sm_count, cudaStream_t s);
-cudaError_t launch_stats_finish(const int64_t* counts, int depth, splat_trace_stats_t* stats, const int32_t* err,
-                                cudaStream_t s);
+// light-map splat of the queued diffuse rays, one thread per (ray, sample)
+cudaError_t launch_splat(const RaySoA& q, const int64_t* d_count, const splat_ftri_t* tris, const SplatParams& sp,
+                         splat_trace_stats_t* stats, int sm_count, cudaStream_t s);
+cudaError_t launch_stats_finish(const int64_t* counts, int depth, const int64_t* splat_count,
+                                splat_trace_stats_t* stats, const int32_t* err, cudaStream_t s);
 cudaError_t launch_unpack_hits(const uint64_t* tmp, int64_t n, const int64_t* d_count, int32_t* hit_idx,
                                float* hit_t, cudaStream_t s);
 
