@@ -412,6 +412,15 @@ static SplatParams make_splat(const float* spectrum, int32_t n_lambda, int64_t u
     // upres(N), src/alg_types.jl:108
     for (int k = 1; k <= sp.n_delta; ++k)
         sp.deltas[k - 1] = ((float)k / (float)sp.n_delta - 0.5f) - (1.0f / (2.0f * (float)sp.n_delta));
+    sp.n_samples = (n_lambda > 0 ? n_lambda : 1) * sp.n_delta * sp.n_delta;
+    // splat kernel: one lane per (ray, plane)
+    const int planes = n_lambda > 0 ? n_lambda : 1;
+    int l2 = 0;
+    while ((1 << l2) < planes && l2 < 5) ++l2;
+    sp.lanes_log2 = l2;
+    sp.chunks = (planes + (1 << l2) - 1) >> l2;
+    sp.inv_nd = 1.0f / (float)sp.n_delta;
+    sp.inv_nd2 = 1.0f / (float)(sp.n_delta * sp.n_delta);
     return sp;
 }
 
@@ -424,6 +433,8 @@ static splat_status_t check_map(const float* spectrum, int32_t n_lambda, int64_t
     if (accum != SPLAT_ACCUM_F32 && accum != SPLAT_ACCUM_I32) return fail(SPLAT_ERR_INVALID, "unknown accumulation");
     if (frac_bits < 0 || frac_bits > 30) return fail(SPLAT_ERR_INVALID, "frac_bits must be 0..30");
     if (w < 1 || h < 1 || w > (1 << 24) || h > (1 << 24)) return fail(SPLAT_ERR_INVALID, "bad light map size");
+    if (w * h * (int64_t)(n_lambda > 0 ? n_lambda : 1) >= (int64_t(1) << 31))
+        return fail(SPLAT_ERR_INVALID, "light map larger than 2^31 texels");
     return SPLAT_OK;
 }
 

@@ -266,31 +266,84 @@ cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_
     return cudaGetLastError();
 }
 
-// One thread per (queued diffuse ray, sample); loops over warp-sized chunks
-// so every lane of a warp reaches the aggregated atomics together.
-__global__ void __launch_bounds__(256) splat_kernel(RaySoA q, const int64_t* __restrict__ d_count,
+// Queued diffuse rays -> light map.  One lane per (ray, wavelength plane):
+// 1 << lanes_log2 lanes share a ray (several rays per warp when it has fewer
+// than 32 planes).  A lane walks its plane's N x N sub-samples in the
+// reference's order (x offset fastest), reusing the first terms of the
+// expansions' left fold (pos + dp/dlambda dlambda, identical bits), and adds
+// runs of samples that land on the same texel in a register before one
+// atomic.  Integer maps are therefore bit-exact; float maps change only the
+// summation order, which float atomics never fix anyway.
+__device__ __forceinline__ void flush_texel(const SplatParams& sp, int32_t off, int32_t vi, float vf) {
+    if (off < 0) return;
+    if (sp.accum == SPLAT_ACCUM_I32)
+        atomicAdd(reinterpret_cast<int*>(sp.map) + off, vi);
+    else
+        atomicAdd(reinterpret_cast<float*>(sp.map) + off, vf);
+}
+
+__global__ void __launch_bounds__(256, 3) splat_kernel(RaySoA q, const int64_t* __restrict__ d_count,
                                                     const splat_ftri_t* __restrict__ tris, SplatParams sp,
                                                     splat_trace_stats_t* st) {
     const int64_t n = *d_count;
-    const int S = (sp.n_lambda > 0 ? sp.n_lambda : 1) * sp.n_delta * sp.n_delta;
-    const int64_t total = n * S;
+    const int lane = lane_id();
+    const int lpr = 1 << sp.lanes_log2;
+    const int rpw = 32 >> sp.lanes_log2;
+    const int sub = lane >> sp.lanes_log2;
+    const int sl = lane & (lpr - 1);
+    const int planes = sp.n_lambda > 0 ? sp.n_lambda : 1;
+    const int nd = sp.n_delta;
+    const int32_t W = (int32_t)sp.w, H = (int32_t)sp.h;
+    const float Wf = (float)W, Hf = (float)H;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     int done = 0;
-    for (int64_t base = warp * 32; base < total; base += n_warps * 32) {
-        const int64_t g = base + lane_id();
-        bool ok = false;
-        int64_t off = 0;
-        float inten = 0.f;
-        if (g < total) {
-            const int64_t k = g / S;
-            const int s = (int)(g - k * S);
-            const RayState r = load_ray(q, k);
-            const Tri T = load_tri(tris, r.ignore);
-            ok = sample_of(sp, r, T, s, off, inten);
+    for (int64_t r0 = warp * rpw; r0 < n; r0 += n_warps * rpw) {
+        const int64_t k = r0 + sub;
+        if (k >= n) continue;
+        const RayState r = load_ray(q, k);
+        const Tri T = load_tri(tris, r.ignore);
+        const TriUV quv = tri_uv(T);
+        for (int il = sl; il < planes; il += lpr) {
+            const float lam = sp.n_lambda > 0 ? sp.spectrum[il] : r.lam;
+            const float dl = lam - r.lam;
+            const F3 pe = r.pos + r.dpl * dl;
+            const F3 de = r.dir + r.ddl * dl;
+            const int32_t plane_off = il * W * H;
+            int32_t run_off = -1, run_i = 0;
+            float run_f = 0.f;
+            for (int iy = 0; iy < nd; ++iy) {
+                const float dy = (r.y + sp.deltas[iy]) - r.y;
+                for (int ix = 0; ix < nd; ++ix) {
+                    const float dx = (r.x + sp.deltas[ix]) - r.x;
+                    const F3 pos = (pe + r.dpx * dx) + r.dpy * dy;
+                    const F3 dir = (de + r.ddx * dx) + r.ddy * dy;
+                    const float bu = dot(quv.N, cross(quv.e1, pos - T.b)) / quv.denom;
+                    const float bv = dot(quv.N, cross(quv.e2, pos - T.c)) / quv.denom;
+                    const float bw = (1.0f - bu) - bv;
+                    const float U = (T.ta.x * bu + T.tb.x * bv) + T.tc.x * bw;
+                    const float V = (T.ta.y * bu + T.tb.y * bv) + T.tc.y * bw;
+                    if (isnan(U) || isnan(V) || isinf(U) || isinf(V)) continue;
+                    const float ci = fminf(fmaxf(ceilf(U * Wf), 1.0f), Wf);
+                    const float cj = fminf(fmaxf(ceilf(V * Hf), 1.0f), Hf);
+                    const int32_t off = plane_off + ((int32_t)ci - 1) + ((int32_t)cj - 1) * W;
+                    const F3 nn = (T.na * bu + T.nb * bv) + T.nc * bw;
+                    const float inten = fabsf(dot(normalize(nn), normalize(dir)));
+                    ++done;
+                    const int32_t vi = __float2int_rn(inten * sp.scale);
+                    if (off == run_off) {
+                        run_i += vi;
+                        run_f += inten;
+                    } else {
+                        flush_texel(sp, run_off, run_i, run_f);
+                        run_off = off;
+                        run_i = vi;
+                        run_f = inten;
+                    }
+                }
+            }
+            flush_texel(sp, run_off, run_i, run_f);
         }
-        accumulate_warp(sp, ok, off, inten);
-        done += ok ? 1 : 0;
     }
     add_stats(st, 0, done);
 }
@@ -298,8 +351,8 @@ __global__ void __launch_bounds__(256) splat_kernel(RaySoA q, const int64_t* __r
 cudaError_t launch_splat(const RaySoA& q, const int64_t* d_count, const splat_ftri_t* tris, const SplatParams& sp,
                          splat_trace_stats_t* stats, int sm_count, cudaStream_t s) {
     if (q.cap <= 0) return cudaSuccess;
-    const int S = (sp.n_lambda > 0 ? sp.n_lambda : 1) * sp.n_delta * sp.n_delta;
-    int64_t b = (q.cap * S + 255) / 256;
+    const int rpw = 32 >> sp.lanes_log2;
+    int64_t b = (q.cap + (int64_t)rpw * 8 - 1) / ((int64_t)rpw * 8);
     const int64_t lim = (int64_t)sm_count * 8;
     if (b > lim) b = lim;
     splat_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_count, tris, sp, stats);

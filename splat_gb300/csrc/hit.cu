@@ -98,6 +98,35 @@ __device__ __forceinline__ HitRay load_hit_ray(const RaySrc& s, int64_t k) {
     return r;
 }
 
+// Plane terms of distance_to_plane (src/geo.jl:433-435) and a conservative
+// pre-test: an accepted hit has t = num / den > 0 (so num, den are non-zero
+// with one sign) and t <= best; |num| > |den| best (1 + 2^-20), evaluated in
+// binary32, implies fl(num / den) > best whatever the roundings.  Triangles
+// failing the pre-test could never be accepted, so skipping them leaves the
+// result bit-identical.
+__device__ __forceinline__ bool tri_candidate(const float4& q0, const HitRay& r, float best, float& num, float& den) {
+    num = q0.w - ((q0.x * r.ox + q0.y * r.oy) + q0.z * r.oz);
+    den = (q0.x * r.dx + q0.y * r.dy) + q0.z * r.dz;
+    const bool same_sign = ((num > 0.0f) & (den > 0.0f)) | ((num < 0.0f) & (den < 0.0f));
+    return same_sign & !(fabsf(num) > (fabsf(den) * best) * (1.0f + 0x1p-20f));
+}
+
+// The rest of the reference's test on one hoisted record (src/geo.jl:433-466).
+__device__ __forceinline__ float tri_t_from(float num, float den, const float4& q1, const float4& q2,
+                                            const float4& q3, const float4& q4, const HitRay& r, bool& inside) {
+    float t = num / den;
+    float px = r.ox + r.dx * t;
+    float py = r.oy + r.dy * t;
+    float pz = r.oz + r.dz * t;
+    float v2x = px - q1.x, v2y = py - q1.y, v2z = pz - q1.z;
+    float d02 = (q2.x * v2x + q2.y * v2y) + q2.z * v2z;
+    float d12 = (q3.x * v2x + q3.y * v2y) + q3.z * v2z;
+    float u = (q3.w * d02 - q4.x * d12) * q4.y;
+    float v = (q2.w * d12 - q4.x * d02) * q4.y;
+    inside = (u >= 0.0f) & (v >= 0.0f) & (u + v < 1.0f);
+    return t;
+}
+
 // The reference's test on one hoisted record (src/geo.jl:433-466).
 __device__ __forceinline__ float tri_t(const float4& q0, const float4& q1, const float4& q2, const float4& q3,
                                        const float4& q4, const HitRay& r, bool& inside) {
@@ -190,15 +219,14 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
 #pragma unroll 2
         for (int j = 0; j < cnt; ++j) {
             const float4 q0 = tile[j].n_nv;
-            const float4 q1 = tile[j].a_idx;
-            const float4 q2 = tile[j].e0;
-            const float4 q3 = tile[j].e1;
-            const float4 q4 = tile[j].inv;
-            const int32_t idx = __float_as_int(q1.w);
 #pragma unroll
             for (int r = 0; r < RPT; ++r) {
+                float num, den;
+                if (!tri_candidate(q0, ray[r], best[r], num, den)) continue;
+                const float4 q1 = tile[j].a_idx;
+                const int32_t idx = __float_as_int(q1.w);
                 bool inside;
-                const float t = tri_t(q0, q1, q2, q3, q4, ray[r], inside);
+                const float t = tri_t_from(num, den, q1, tile[j].e0, tile[j].e1, tile[j].inv, ray[r], inside);
                 if (inside & (t > 0.0f) & (idx != ray[r].ig) & (t < best[r])) {
                     best[r] = t;
                     bi[r] = idx;
@@ -492,11 +520,12 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh_kernel(RaySrc src, BvhVie
                 const int count = (enc & 15) + 1;
                 for (int j = 0; j < count; ++j) {
                     const TriHit* h = bvh.tris + first + j;
-                    const float4 q0 = __ldg(&h->n_nv), q1 = __ldg(&h->a_idx), q2 = __ldg(&h->e0),
-                                 q3 = __ldg(&h->e1), q4 = __ldg(&h->inv);
+                    float num, den;
+                    if (!tri_candidate(__ldg(&h->n_nv), r, best, num, den)) continue;
+                    const float4 q1 = __ldg(&h->a_idx);
                     const int32_t idx = __float_as_int(q1.w);
                     bool inside;
-                    const float t = tri_t(q0, q1, q2, q3, q4, r, inside);
+                    const float t = tri_t_from(num, den, q1, __ldg(&h->e0), __ldg(&h->e1), __ldg(&h->inv), r, inside);
                     if (inside & (t > 0.0f) & (idx != r.ig) & ((t < best) | ((t == best) & (idx < bi)))) {
                         best = t;
                         bi = idx;

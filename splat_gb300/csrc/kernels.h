@@ -78,6 +78,10 @@ struct SplatParams {
     int64_t w, h;
     int32_t n_lambda;  // 0: own wavelength
     int32_t n_delta;
+    int32_t n_samples;   // planes x n_delta^2 per ray
+    int32_t lanes_log2;  // lanes per ray in the splat kernel = 1 << lanes_log2 (<= 32)
+    int32_t chunks;      // sample chunks per lane
+    float inv_nd, inv_nd2;  // 1 / n_delta, 1 / n_delta^2 (index decode)
     float spectrum[SPLAT_MAX_LAMBDA];
     float deltas[16];
 };

@@ -262,6 +262,41 @@ __device__ __forceinline__ void final_evolution(const RayState& r, const HitDeri
     o.ignore = i;
 }
 
+// Triangle-only terms of reverse_uv (src/geo.jl:236-252), hoisted out of a
+// ray's samples: identical values, computed once.
+struct TriUV {
+    F3 N, e1, e2;  // cross(b - a, c - a), c - b, a - c
+    float denom;   // dot(N, N)
+};
+__device__ __forceinline__ TriUV tri_uv(const Tri& T) {
+    TriUV q;
+    q.N = cross(T.b - T.a, T.c - T.a);
+    q.denom = dot(q.N, q.N);
+    q.e1 = T.c - T.b;
+    q.e2 = T.a - T.c;
+    return q;
+}
+
+// splat_sample with the hoisted triangle terms.
+__device__ __forceinline__ bool splat_sample_uv(const RayState& r, const Tri& T, const TriUV& q, float lam, float xs,
+                                                float ys, int64_t W, int64_t H, int64_t& off_ij, float& intensity) {
+    F3 pos = p_expansion(r, lam, xs, ys);
+    F3 dir = d_expansion(r, lam, xs, ys);
+    const float bu = dot(q.N, cross(q.e1, pos - T.b)) / q.denom;
+    const float bv = dot(q.N, cross(q.e2, pos - T.c)) / q.denom;
+    float bw = (1.0f - bu) - bv;
+    float U = (T.ta.x * bu + T.tb.x * bv) + T.tc.x * bw;
+    float Vt = (T.ta.y * bu + T.tb.y * bv) + T.tc.y * bw;
+    if (isnan(U) || isnan(Vt) || isinf(U) || isinf(Vt)) return false;
+    float ci = ceilf(U * (float)W), cj = ceilf(Vt * (float)H);
+    ci = fminf(fmaxf(ci, 1.0f), (float)W);
+    cj = fminf(fmaxf(cj, 1.0f), (float)H);
+    off_ij = ((int64_t)ci - 1) + ((int64_t)cj - 1) * W;
+    F3 n = (T.na * bu + T.nb * bv) + T.nc * bw;
+    intensity = fabsf(dot(normalize(n), normalize(dir)));
+    return true;
+}
+
 // One sample of atomic_spectrum_kernel2 (src/ray_imagers.jl:78-113):
 // expand -> tex_uv -> texel -> cosine_shading.  False when uv is not finite.
 __device__ __forceinline__ bool splat_sample(const RayState& r, const Tri& T, float lam, float xs, float ys,

@@ -104,3 +104,35 @@ def test_edge_cases(torch_cuda):
         hit, _ = _hits(tracer, one, hitter, rays)
         assert np.array_equal(hit, o1)
     del empty
+
+
+def test_degenerate_geometry_matches_oracle(torch_cuda):
+    """Rays starting on triangle planes (num = 0), running parallel to them
+    (den = 0), coincident cube faces (exact ties) and grazing hits: brute and
+    BVH both equal the oracle."""
+    from splat_gb300 import scenes as S
+    from splat_gb300 import tracer
+    from splat_gb300 import types as T
+
+    tris, fd = S.assemble(S.menger_tris(2, 2.0, rotation_seed=None), S.box_tris(3.0))
+    scene = tracer.Scene(tris, fd, bvh=True)
+    rng = np.random.default_rng(17)
+    n = 6000
+    rays = np.zeros(n, dtype=T.ADRAY)
+    grid = np.round(rng.uniform(-1, 1, size=(n, 3)) * 9) / 9  # on the sponge's cube planes
+    d = rng.normal(size=(n, 3))
+    axis = rng.integers(0, 3, size=n)
+    par = rng.uniform(size=n) < 0.3
+    d[par, axis[par]] = 0.0  # parallel to a family of planes
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays["pos"] = grid.astype(np.float32)
+    rays["dir"] = d.astype(np.float32)
+    rays["ignore_tri"] = np.where(rng.uniform(size=n) < 0.5, rng.integers(2, tris.shape[0] + 1, size=n), 1)
+    rays["status"] = T.STATUS_ACTIVE
+    o_hit, o_t = O.next_hit(rays, tris)
+    for hitter in (tracer.BRUTE, tracer.BVH):
+        hit, t = _hits(tracer, scene, hitter, rays)
+        bad = np.nonzero(hit != o_hit)[0]
+        assert bad.size == 0, f"hitter {hitter}: {bad[:10]} {hit[bad[:5]]} vs {o_hit[bad[:5]]}"
+        assert np.array_equal(t.view(np.uint32), o_t.view(np.uint32))
+    assert (o_hit > 1).mean() > 0.5
