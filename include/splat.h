@@ -200,6 +200,28 @@ splat_status_t splat_rays_from_light(const splat_rect_light_t* light, int64_t up
 splat_status_t splat_next_hit_brute(const splat_adray_t* d_rays, int64_t n_rays, const splat_ntri_t* d_n_tris,
                                     int64_t n_tris, uint64_t* d_tmp, int32_t* d_hit_idx, void* stream);
 
+/* Allocation-free variant of splat_next_hit_brute.  No counterpart in the
+ * reference: it exists for callers that cannot allocate device memory at the
+ * point of the call -- a render callback running under a fixed, pre-admitted
+ * memory budget, a Julia finalizer or @cfunction callback where triggering the
+ * CUDA.jl allocator (and the garbage collection and synchronisation it may
+ * cause) is not allowed, or a host that hands out only the input and output
+ * buffers.  The packed (t, index) words that splat_next_hit_brute keeps in the
+ * caller's d_tmp live instead in one array of SPLAT_STATIC_HIT_MAX_RAYS
+ * 64-bit words (4 MiB) inside the library, which every GPU that loads the
+ * library holds until the process exits.  Rules:
+ *   - n_rays above SPLAT_STATIC_HIT_MAX_RAYS is rejected (SPLAT_ERR_INVALID);
+ *   - the first call on a device looks the array's device address up (once
+ *     per device, with that device current); make that first call before
+ *     any stream capture;
+ *   - every call shares the array and first resets the words it uses, so
+ *     calls whose kernels overlap on the GPU (other streams, other host
+ *     threads) race and must be serialised by the caller;
+ *   - no cudaMalloc, cudaFree or allocating library routine is called. */
+#define SPLAT_STATIC_HIT_MAX_RAYS (1 << 19)
+splat_status_t splat_next_hit_brute_static(const splat_adray_t* d_rays, int64_t n_rays, const splat_ntri_t* d_n_tris,
+                                           int64_t n_tris, int32_t* d_hit_idx, void* stream);
+
 /* next_hit! with a resident scene (brute force or BVH,
  * src/hitters.jl:205-226 / 615-647).  d_hit_t (optional) receives the hit
  * distance, Inf on a miss. */

@@ -13,6 +13,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libsplat.so")
 
 MAX_LAMBDA = 64
+STATIC_HIT_MAX_RAYS = 1 << 19
 
 OK = 0
 ERR_INVALID = 1
@@ -84,6 +85,7 @@ SIGNATURES = {
     "splat_scene_tris": ([vp], vp),
     "splat_rays_from_light": ([C.POINTER(RectLight), i64, C.POINTER(LambdaMode), u64, u32, vp, vp], i32),
     "splat_next_hit_brute": ([vp, i64, vp, i64, vp, vp, vp], i32),
+    "splat_next_hit_brute_static": ([vp, i64, vp, i64, vp, vp], i32),
     "splat_next_hit": ([vp, i32, vp, i64, vp, vp, vp], i32),
     "splat_run_evolution_workspace_size": ([i64], sz),
     "splat_run_evolution": ([vp, i32, vp, i64, i32, C.POINTER(Material), f32, u64, u32, vp, vp, sz, vp], i32),

@@ -363,6 +363,23 @@ splat_status_t splat_next_hit_brute(const splat_adray_t* d_rays, int64_t n_rays,
     return SPLAT_OK;
 }
 
+splat_status_t splat_next_hit_brute_static(const splat_adray_t* d_rays, int64_t n_rays, const splat_ntri_t* d_n_tris,
+                                           int64_t n_tris, int32_t* d_hit_idx, void* stream) {
+    if (n_rays < 0 || n_tris < 0) return fail(SPLAT_ERR_INVALID, "next_hit_brute_static: negative size");
+    if (n_rays > SPLAT_STATIC_HIT_MAX_RAYS)
+        return fail(SPLAT_ERR_INVALID, "next_hit_brute_static: n_rays " + std::to_string(n_rays) +
+                                           " exceeds the static scratch of " +
+                                           std::to_string(SPLAT_STATIC_HIT_MAX_RAYS) + " rays");
+    if (n_rays == 0) return SPLAT_OK;
+    if (!d_rays || !d_hit_idx || (n_tris > 0 && !d_n_tris))
+        return fail(SPLAT_ERR_INVALID, "next_hit_brute_static: null pointer");
+    ProfScope ps(SPLAT_KERNEL_HIT_BRUTE, reinterpret_cast<cudaStream_t>(stream));
+    SPLAT_CUDA(launch_hit_brute_ntris_static(d_rays, n_rays, d_n_tris, n_tris, d_hit_idx, sm_count_current(),
+                                             reinterpret_cast<cudaStream_t>(stream)),
+               "next_hit_brute_static");
+    return SPLAT_OK;
+}
+
 static splat_status_t hit_any(const splat_scene_t* s, int32_t hitter, const RaySrc& src, int64_t cap,
                               int32_t* hit_idx, float* hit_t, uint64_t* tmp, cudaStream_t st) {
     cudaError_t e;

@@ -16,6 +16,7 @@
 //   succeed is visited, and the same lexicographic rule makes the result
 //   identical to brute force.
 #include <cstdio>
+#include <mutex>
 
 #include "kernels.h"
 
@@ -444,6 +445,48 @@ cudaError_t launch_hit_brute_ntris(const splat_adray_t* rays, int64_t n_rays, co
         if (e != cudaSuccess) return e;
     }
     return launch_unpack_hits(tmp, n_rays, nullptr, hit_idx, nullptr, s);
+}
+
+// ---------------------------------------------------------------------------
+// brute force over n_tris with library-held scratch (no allocation)
+// ---------------------------------------------------------------------------
+// The packed (t, index) words of splat_next_hit_brute_static live here rather
+// than in caller memory.  Every GPU that loads the library holds this array
+// until the process exits; all calls share it.
+static __device__ __align__(256) unsigned long long g_static_hit_tmp[kStaticHitMaxRays];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+void* g_static_ptr[kMaxDevices] = {nullptr};
+
+// Device address of g_static_hit_tmp on the current device, looked up once
+// per device (host code only has a host-side stand-in for the symbol).
+cudaError_t static_hit_scratch(unsigned long long** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (g_static_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_static_hit_tmp);
+        if (e != cudaSuccess) return e;
+        g_static_ptr[dev] = p;
+    }
+    *out = reinterpret_cast<unsigned long long*>(g_static_ptr[dev]);
+    return cudaSuccess;
+}
+}  // namespace
+
+cudaError_t launch_hit_brute_ntris_static(const splat_adray_t* rays, int64_t n_rays, const splat_ntri_t* ntris,
+                                          int64_t n_tris, int32_t* hit_idx, int sm_count, cudaStream_t s) {
+    unsigned long long* tmp = nullptr;
+    cudaError_t e = static_hit_scratch(&tmp);
+    if (e != cudaSuccess) return e;
+    // launch_hit_brute_ntris first resets the n_rays words it uses to (Inf, 1)
+    return launch_hit_brute_ntris(rays, n_rays, ntris, n_tris, reinterpret_cast<uint64_t*>(tmp), hit_idx, sm_count,
+                                  s);
 }
 
 // ---------------------------------------------------------------------------

@@ -47,6 +47,11 @@ cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs
 // brute force over the reference's n_tris array (Tuple{Int32,Tri})
 cudaError_t launch_hit_brute_ntris(const splat_adray_t* rays, int64_t n_rays, const splat_ntri_t* ntris,
                                    int64_t n_tris, uint64_t* tmp, int32_t* hit_idx, int sm_count, cudaStream_t s);
+// splat_next_hit_brute_static: the same hitter with its scratch in a
+// file-scope device array (no allocation); n_rays <= kStaticHitMaxRays
+constexpr int64_t kStaticHitMaxRays = SPLAT_STATIC_HIT_MAX_RAYS;
+cudaError_t launch_hit_brute_ntris_static(const splat_adray_t* rays, int64_t n_rays, const splat_ntri_t* ntris,
+                                          int64_t n_tris, int32_t* hit_idx, int sm_count, cudaStream_t s);
 cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, int32_t* hit_idx, float* hit_t,
                            int32_t* err, int sm_count, cudaStream_t s);
 
