@@ -108,7 +108,9 @@ typedef struct splat_lambda_mode {
     float lambda1;
 } splat_lambda_mode_t;
 
-enum { SPLAT_HITTER_BRUTE = 0, SPLAT_HITTER_BVH = 1 };
+/* Hitters: BRUTE all pairs; BVH the four-wide BVH; BVH2 the binary BVH it is
+ * collapsed from.  All three return identical results. */
+enum { SPLAT_HITTER_BRUTE = 0, SPLAT_HITTER_BVH = 1, SPLAT_HITTER_BVH2 = 2 };
 enum { SPLAT_ACCUM_F32 = 0, SPLAT_ACCUM_I32 = 1 };
 
 /* flags */

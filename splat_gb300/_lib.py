@@ -24,6 +24,7 @@ ERR_DEVICE = 5
 
 HITTER_BRUTE = 0
 HITTER_BVH = 1
+HITTER_BVH2 = 2
 ACCUM_F32 = 0
 ACCUM_I32 = 1
 FLAG_REF_QUIRKS = 1

@@ -153,6 +153,10 @@ struct splat_scene {
     int32_t* d_order = nullptr;
     int32_t* d_levels = nullptr;
     std::vector<int64_t> level_off;
+    Bvh4Node* d_nodes4 = nullptr;
+    int64_t n_nodes4 = 0;
+    int32_t* d_levels4 = nullptr;
+    std::vector<int64_t> level4_off;
     int depth = 0, max_leaf = 0;
     int64_t leaves = 0;
     float pad_abs = 0.f, pad_rel = 0.f;
@@ -169,6 +173,8 @@ static void scene_free(splat_scene* s) {
     cudaFree(s->d_bvh);
     cudaFree(s->d_order);
     cudaFree(s->d_levels);
+    cudaFree(s->d_nodes4);
+    cudaFree(s->d_levels4);
     cudaFree(s->d_err);
     delete s;
 }
@@ -188,6 +194,14 @@ static splat_status_t scene_pack(splat_scene* s, cudaStream_t st) {
             const int64_t a = s->level_off[l], b = s->level_off[l + 1];
             e = launch_refit_level(s->d_nodes, s->d_levels + a, b - a, s->d_bvh, s->d_ftri, s->pad_abs, s->pad_rel, st);
             if (e != cudaSuccess) return cuda_fail(e, "BVH refit");
+        }
+    }
+    if (s->d_nodes4) {
+        for (size_t l = 0; l + 1 < s->level4_off.size(); ++l) {
+            const int64_t a = s->level4_off[l], b = s->level4_off[l + 1];
+            e = launch_refit4_level(s->d_nodes4, s->d_levels4 + a, b - a, s->d_bvh, s->d_ftri, s->pad_abs, s->pad_rel,
+                                    st);
+            if (e != cudaSuccess) return cuda_fail(e, "BVH4 refit");
         }
     }
     return SPLAT_OK;
@@ -257,6 +271,10 @@ splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris,
         chk(dalloc(&s->d_bvh, sizeof(TriHit) * (size_t)s->n_recs, s->bytes));
         chk(dalloc(&s->d_order, sizeof(int32_t) * bvh.order.size(), s->bytes));
         chk(dalloc(&s->d_levels, sizeof(int32_t) * bvh.level_nodes.size(), s->bytes));
+        s->n_nodes4 = (int64_t)bvh.nodes4.size();
+        chk(dalloc(&s->d_nodes4, sizeof(Bvh4Node) * bvh.nodes4.size(), s->bytes));
+        chk(dalloc(&s->d_levels4, sizeof(int32_t) * bvh.level4_nodes.size(), s->bytes));
+        s->level4_off = bvh.level4_off;
         s->level_off = bvh.level_off;
         s->depth = bvh.depth;
         s->max_leaf = bvh.max_leaf;
@@ -276,6 +294,10 @@ splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris,
         chk(cudaMemcpyAsync(s->d_order, bvh.order.data(), sizeof(int32_t) * bvh.order.size(), cudaMemcpyHostToDevice,
                             st));
         chk(cudaMemcpyAsync(s->d_levels, bvh.level_nodes.data(), sizeof(int32_t) * bvh.level_nodes.size(),
+                            cudaMemcpyHostToDevice, st));
+        chk(cudaMemcpyAsync(s->d_nodes4, bvh.nodes4.data(), sizeof(Bvh4Node) * bvh.nodes4.size(),
+                            cudaMemcpyHostToDevice, st));
+        chk(cudaMemcpyAsync(s->d_levels4, bvh.level4_nodes.data(), sizeof(int32_t) * bvh.level4_nodes.size(),
                             cudaMemcpyHostToDevice, st));
     }
     if (e == cudaSuccess) chk(launch_pack_hits(s->d_ftri, n_tris, s->d_brute, s->d_order, s->d_bvh, st));
@@ -383,11 +405,15 @@ splat_status_t splat_next_hit_brute_static(const splat_adray_t* d_rays, int64_t 
 static splat_status_t hit_any(const splat_scene_t* s, int32_t hitter, const RaySrc& src, int64_t cap,
                               int32_t* hit_idx, float* hit_t, uint64_t* tmp, cudaStream_t st) {
     cudaError_t e;
-    ProfScope ps(hitter == SPLAT_HITTER_BVH && s->d_nodes ? SPLAT_KERNEL_HIT_BVH : SPLAT_KERNEL_HIT_BRUTE, st);
-    if (hitter == SPLAT_HITTER_BVH) {
+    const bool bvh = hitter == SPLAT_HITTER_BVH || hitter == SPLAT_HITTER_BVH2;
+    ProfScope ps(bvh && s->d_nodes ? SPLAT_KERNEL_HIT_BVH : SPLAT_KERNEL_HIT_BRUTE, st);
+    if (bvh) {
         if (!s->d_nodes) {
             if (s->n_recs > 0) return fail(SPLAT_ERR_INVALID, "BVH hitter on a scene created without BVH");
             e = launch_hit_brute(src, cap, s->d_brute, 0, hit_idx, hit_t, nullptr, s->d_err, sm_count_current(), st);
+        } else if (hitter == SPLAT_HITTER_BVH) {
+            e = launch_hit_bvh4(src, cap, Bvh4View{s->d_nodes4, s->d_bvh}, hit_idx, hit_t, s->d_err,
+                                sm_count_current(), st);
         } else {
             e = launch_hit_bvh(src, cap, BvhView{s->d_nodes, s->d_bvh}, hit_idx, hit_t, s->d_err, sm_count_current(),
                                st);
@@ -550,7 +576,7 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
     splat_status_t rc =
         check_map(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
     if (rc != SPLAT_OK) return rc;
-    if (P->hitter == SPLAT_HITTER_BVH && !scene->d_nodes && scene->n_recs > 0)
+    if ((P->hitter == SPLAT_HITTER_BVH || P->hitter == SPLAT_HITTER_BVH2) && !scene->d_nodes && scene->n_recs > 0)
         return fail(SPLAT_ERR_INVALID, "trace_forward: BVH hitter on a scene without BVH");
     const int64_t n_grid = grid_rays(P);
     const int64_t rb = P->ray_begin < 0 ? 0 : P->ray_begin;

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <functional>
 
 namespace splat {
 
@@ -287,6 +288,71 @@ bool build_bvh(const splat_ftri_t* tris, int64_t n_tris, BvhHost& out, std::stri
     }
     out.max_leaf = max_leaf;
     out.leaves = leaves;
+
+    // Collapse into a four-wide tree: starting from a binary node's two
+    // children, repeatedly open the inner child with the largest surface area
+    // until four children are reached or only leaves remain.
+    std::vector<int> depth4_of;
+    std::function<int(int, int)> emit = [&](int b, int depth) -> int {
+        std::vector<int> ch = {B.nodes[(size_t)b].left, B.nodes[(size_t)b].right};
+        while (ch.size() < 4) {
+            int pick = -1;
+            float best_area = -1.0f;
+            for (size_t i = 0; i < ch.size(); ++i) {
+                const BNode& c = B.nodes[(size_t)ch[i]];
+                if (c.count == 0 && c.box.area() > best_area) {
+                    best_area = c.box.area();
+                    pick = (int)i;
+                }
+            }
+            if (pick < 0) break;
+            const int c = ch[(size_t)pick];
+            ch.erase(ch.begin() + pick);
+            ch.push_back(B.nodes[(size_t)c].left);
+            ch.push_back(B.nodes[(size_t)c].right);
+        }
+        const int me = (int)out.nodes4.size();
+        out.nodes4.emplace_back();
+        depth4_of.push_back(depth);
+        int refs[4] = {0, 0, 0, 0};
+        for (size_t i = 0; i < ch.size(); ++i)
+            refs[i] = B.nodes[(size_t)ch[i]].count > 0 ? ref_of(ch[i]) : emit(ch[i], depth + 1);
+        Bvh4Node& f = out.nodes4[(size_t)me];
+        float lo[3][4], hi[3][4];
+        for (int a = 0; a < 3; ++a)
+            for (int i = 0; i < 4; ++i) {
+                lo[a][i] = INFINITY;
+                hi[a][i] = -INFINITY;
+            }
+        for (size_t i = 0; i < ch.size(); ++i)
+            for (int a = 0; a < 3; ++a) {
+                lo[a][i] = B.nodes[(size_t)ch[i]].box.lo[a];
+                hi[a][i] = B.nodes[(size_t)ch[i]].box.hi[a];
+            }
+        f.lox = make_float4(lo[0][0], lo[0][1], lo[0][2], lo[0][3]);
+        f.hix = make_float4(hi[0][0], hi[0][1], hi[0][2], hi[0][3]);
+        f.loy = make_float4(lo[1][0], lo[1][1], lo[1][2], lo[1][3]);
+        f.hiy = make_float4(hi[1][0], hi[1][1], hi[1][2], hi[1][3]);
+        f.loz = make_float4(lo[2][0], lo[2][1], lo[2][2], lo[2][3]);
+        f.hiz = make_float4(hi[2][0], hi[2][1], hi[2][2], hi[2][3]);
+        f.c = make_int4(refs[0], refs[1], refs[2], refs[3]);
+        f.meta = make_int4((int)ch.size(), 0, 0, 0);
+        return me;
+    };
+    emit(0, 0);
+    int maxd4 = 0;
+    for (int d : depth4_of) maxd4 = std::max(maxd4, d);
+    out.depth4 = maxd4 + 1;
+    out.level4_off.assign(1, 0);
+    for (int d = maxd4; d >= 0; --d) {
+        for (size_t q = 0; q < depth4_of.size(); ++q)
+            if (depth4_of[q] == d) out.level4_nodes.push_back((int32_t)q);
+        out.level4_off.push_back((int64_t)out.level4_nodes.size());
+    }
+    if (3 * out.depth4 + 1 >= kBvhStack) {
+        err = "four-wide BVH deeper than the traversal stack";
+        return false;
+    }
     return true;
 }
 

@@ -17,6 +17,11 @@ struct BvhHost {
     int max_leaf = 0;
     int64_t leaves = 0;
     float pad_abs = 0.f, pad_rel = 0.f;
+    // four-wide tree collapsed from the binary one (same leaves)
+    std::vector<Bvh4Node> nodes4;
+    std::vector<int32_t> level4_nodes;
+    std::vector<int64_t> level4_off;
+    int depth4 = 0;
 };
 
 bool build_bvh(const splat_ftri_t* tris, int64_t n_tris, BvhHost& out, std::string& err);

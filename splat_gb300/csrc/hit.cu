@@ -604,6 +604,137 @@ cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, 
 }
 
 // ---------------------------------------------------------------------------
+// four-wide BVH traversal
+// ---------------------------------------------------------------------------
+// One thread per ray.  A node fetch (128 bytes) tests four child boxes; the
+// hit children are sorted by entry distance, the nearest is visited next and
+// the others are pushed farthest first together with their entry distance,
+// so a popped entry that lies beyond the current best hit is skipped.
+__device__ __forceinline__ float comp(const float4& v, int i) {
+    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+#define SPLAT_CSWAP(ka, ra, kb, rb)       \
+    if (kb < ka) {                         \
+        const float tk = ka;               \
+        ka = kb;                           \
+        kb = tk;                           \
+        const int tr = ra;                 \
+        ra = rb;                           \
+        rb = tr;                           \
+    }
+
+template <bool AOS>
+__global__ void __launch_bounds__(kBvhThreads) hit_bvh4_kernel(RaySrc src, Bvh4View bvh,
+                                                               int32_t* __restrict__ hit_idx,
+                                                               float* __restrict__ hit_t, int32_t* err) {
+    const int64_t n = src.d_count ? *src.d_count : src.n;
+    const float kInf = __int_as_float(0x7f800000);
+    const float kMax = 3.402823466e38f;
+    int stack_ref[kBvhStack];
+    float stack_t[kBvhStack];
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const HitRay r = load_hit_ray<AOS>(src, k);
+        const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
+        const float oix = r.ox * ix, oiy = r.oy * iy, oiz = r.oz * iz;
+        float best = kInf;
+        int32_t bi = 1;
+        int sp = 0;
+        int ref = 0;
+        while (true) {
+            if (ref >= 0) {
+                const Bvh4Node* nd = bvh.nodes + ref;
+                const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix);
+                const float4 ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
+                const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+                const int4 c = __ldg(&nd->c);
+                const int nc = __ldg(&nd->meta.x);
+                float key[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float a0 = fmaf(comp(lx, i), ix, -oix), b0 = fmaf(comp(hx, i), ix, -oix);
+                    const float a1 = fmaf(comp(ly, i), iy, -oiy), b1 = fmaf(comp(hy, i), iy, -oiy);
+                    const float a2 = fmaf(comp(lz, i), iz, -oiz), b2 = fmaf(comp(hz, i), iz, -oiz);
+                    const float tmin = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fminf(a2, b2));
+                    const float tmax = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fmaxf(a2, b2));
+                    const bool h = (i < nc) & (tmin <= tmax) & (tmax >= 0.0f) & (tmin <= best);
+                    key[i] = h ? fminf(tmin, kMax) : kInf;
+                }
+                float k0 = key[0], k1 = key[1], k2 = key[2], k3 = key[3];
+                int r0 = c.x, r1 = c.y, r2 = c.z, r3 = c.w;
+                SPLAT_CSWAP(k0, r0, k1, r1);
+                SPLAT_CSWAP(k2, r2, k3, r3);
+                SPLAT_CSWAP(k0, r0, k2, r2);
+                SPLAT_CSWAP(k1, r1, k3, r3);
+                SPLAT_CSWAP(k1, r1, k2, r2);
+                if (k0 < kInf) {
+                    if (sp + 3 <= kBvhStack) {
+                        if (k3 < kInf) {
+                            stack_ref[sp] = r3;
+                            stack_t[sp++] = k3;
+                        }
+                        if (k2 < kInf) {
+                            stack_ref[sp] = r2;
+                            stack_t[sp++] = k2;
+                        }
+                        if (k1 < kInf) {
+                            stack_ref[sp] = r1;
+                            stack_t[sp++] = k1;
+                        }
+                    } else {
+                        atomicOr(err, 2);
+                    }
+                    ref = r0;
+                    continue;
+                }
+            } else {
+                const int enc = ~ref;
+                const int first = enc >> 4;
+                const int count = (enc & 15) + 1;
+                for (int j = 0; j < count; ++j) {
+                    const TriHit* h = bvh.tris + first + j;
+                    float num, den;
+                    if (!tri_candidate(__ldg(&h->n_nv), r, best, num, den)) continue;
+                    const float4 q1 = __ldg(&h->a_idx);
+                    const int32_t idx = __float_as_int(q1.w);
+                    bool inside;
+                    const float t = tri_t_from(num, den, q1, __ldg(&h->e0), __ldg(&h->e1), __ldg(&h->inv), r, inside);
+                    if (inside & (t > 0.0f) & (idx != r.ig) & ((t < best) | ((t == best) & (idx < bi)))) {
+                        best = t;
+                        bi = idx;
+                    }
+                }
+            }
+            bool found = false;
+            while (sp > 0) {
+                --sp;
+                if (stack_t[sp] <= best) {
+                    ref = stack_ref[sp];
+                    found = true;
+                    break;
+                }
+            }
+            if (!found) break;
+        }
+        hit_idx[k] = bi;
+        if (hit_t) hit_t[k] = best;
+    }
+}
+#undef SPLAT_CSWAP
+
+cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh, int32_t* hit_idx, float* hit_t,
+                            int32_t* err, int sm_count, cudaStream_t s) {
+    if (cap <= 0) return cudaSuccess;
+    const int grid = grid_for(cap, kBvhThreads, sm_count, 16);
+    if (rays.aos)
+        hit_bvh4_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
+    else
+        hit_bvh4_kernel<false><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // scene packing and BVH refit
 // ---------------------------------------------------------------------------
 __global__ void pack_hits_kernel(const splat_ftri_t* __restrict__ ftri, int64_t n_tris, TriHit* brute,
@@ -679,6 +810,76 @@ __global__ void refit_level_kernel(BvhNode* nodes, const int32_t* __restrict__ l
         nd.y = make_float4(l0[1], h0[1], l1[1], h1[1]);
         nd.z = make_float4(l0[2], h0[2], l1[2], h1[2]);
     }
+}
+
+__device__ __forceinline__ void leaf_box(int ref, const TriHit* recs, const splat_ftri_t* ftri, float pad_abs,
+                                         float pad_rel, float lo[3], float hi[3]) {
+    const int enc = ~ref;
+    const int first = enc >> 4, count = (enc & 15) + 1;
+    for (int j = 0; j < count; ++j) {
+        const int32_t idx = __float_as_int(recs[first + j].a_idx.w);
+        const float* p = ftri[idx - 1].v[1];
+        float tl[3], th[3];
+        for (int a = 0; a < 3; ++a) {
+            tl[a] = fminf(fminf(p[a], p[3 + a]), p[6 + a]);
+            th[a] = fmaxf(fmaxf(p[a], p[3 + a]), p[6 + a]);
+        }
+        const float dx = th[0] - tl[0], dy = th[1] - tl[1], dz = th[2] - tl[2];
+        const float pad = pad_abs + pad_rel * sqrtf(dx * dx + dy * dy + dz * dz);
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = fminf(lo[a], tl[a] - pad);
+            hi[a] = fmaxf(hi[a], th[a] + pad);
+        }
+    }
+}
+
+__global__ void refit4_level_kernel(Bvh4Node* nodes, const int32_t* __restrict__ level_nodes, int64_t n_level,
+                                    const TriHit* __restrict__ recs, const splat_ftri_t* __restrict__ ftri,
+                                    float pad_abs, float pad_rel) {
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n_level; q += (int64_t)gridDim.x * blockDim.x) {
+        Bvh4Node& nd = nodes[level_nodes[q]];
+        const int nc = nd.meta.x;
+        float lo[3][4], hi[3][4];
+        const int refs[4] = {nd.c.x, nd.c.y, nd.c.z, nd.c.w};
+        for (int i = 0; i < 4; ++i) {
+            float l[3] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000)};
+            float h[3] = {-l[0], -l[0], -l[0]};
+            if (i < nc) {
+                if (refs[i] >= 0) {
+                    const Bvh4Node& ch = nodes[refs[i]];
+                    for (int j = 0; j < ch.meta.x; ++j) {
+                        l[0] = fminf(l[0], comp(ch.lox, j));
+                        h[0] = fmaxf(h[0], comp(ch.hix, j));
+                        l[1] = fminf(l[1], comp(ch.loy, j));
+                        h[1] = fmaxf(h[1], comp(ch.hiy, j));
+                        l[2] = fminf(l[2], comp(ch.loz, j));
+                        h[2] = fmaxf(h[2], comp(ch.hiz, j));
+                    }
+                } else {
+                    leaf_box(refs[i], recs, ftri, pad_abs, pad_rel, l, h);
+                }
+            }
+            for (int a = 0; a < 3; ++a) {
+                lo[a][i] = l[a];
+                hi[a][i] = h[a];
+            }
+        }
+        nd.lox = make_float4(lo[0][0], lo[0][1], lo[0][2], lo[0][3]);
+        nd.hix = make_float4(hi[0][0], hi[0][1], hi[0][2], hi[0][3]);
+        nd.loy = make_float4(lo[1][0], lo[1][1], lo[1][2], lo[1][3]);
+        nd.hiy = make_float4(hi[1][0], hi[1][1], hi[1][2], hi[1][3]);
+        nd.loz = make_float4(lo[2][0], lo[2][1], lo[2][2], lo[2][3]);
+        nd.hiz = make_float4(hi[2][0], hi[2][1], hi[2][2], hi[2][3]);
+    }
+}
+
+cudaError_t launch_refit4_level(Bvh4Node* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,
+                                const splat_ftri_t* ftri, float pad_abs, float pad_rel, cudaStream_t s) {
+    if (n_level <= 0) return cudaSuccess;
+    refit4_level_kernel<<<grid_for(n_level, 128, 152, 8), 128, 0, s>>>(nodes, level_nodes, n_level, bvh_recs, ftri,
+                                                                        pad_abs, pad_rel);
+    ++g_launches;
+    return cudaGetLastError();
 }
 
 cudaError_t launch_refit_level(BvhNode* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,

@@ -33,6 +33,20 @@ struct __align__(16) BvhNode {
 };
 static_assert(sizeof(BvhNode) == 64, "BvhNode layout");
 
+// Four-wide node collapsed from the binary tree: child i's box in
+// component i of the six float4s; unused slots have count <= i.
+struct __align__(16) Bvh4Node {
+    float4 lox, hix, loy, hiy, loz, hiz;
+    int4 c;      // child refs (as BvhNode)
+    int4 meta;   // x: number of children (2..4)
+};
+static_assert(sizeof(Bvh4Node) == 128, "Bvh4Node layout");
+
+struct Bvh4View {
+    const Bvh4Node* nodes;
+    const TriHit* tris;  // BVH order (shared with the binary tree)
+};
+
 constexpr int kLeafMax = 16;
 constexpr int kBvhStack = 64;
 
@@ -54,6 +68,10 @@ cudaError_t launch_hit_brute_ntris_static(const splat_adray_t* rays, int64_t n_r
                                           int64_t n_tris, int32_t* hit_idx, int sm_count, cudaStream_t s);
 cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, int32_t* hit_idx, float* hit_t,
                            int32_t* err, int sm_count, cudaStream_t s);
+cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh, int32_t* hit_idx, float* hit_t,
+                            int32_t* err, int sm_count, cudaStream_t s);
+cudaError_t launch_refit4_level(Bvh4Node* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,
+                                const splat_ftri_t* ftri, float pad_abs, float pad_rel, cudaStream_t s);
 
 // scene packing / refit
 cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, const int32_t* bvh_order,

@@ -25,6 +25,7 @@ from . import types as T
 
 BRUTE = L.HITTER_BRUTE
 BVH = L.HITTER_BVH
+BVH2 = L.HITTER_BVH2
 
 
 def _torch():
@@ -237,7 +238,7 @@ def trace_params(wl, ray_begin: int = 0, ray_end: int = 0, zero_map: bool = True
     P.lambda_mode = _lmode(wl.lambda_mode)
     P.seed = int(wl.seed)
     P.depth = int(wl.depth)
-    P.hitter = BVH if wl.hitter == "bvh" else BRUTE
+    P.hitter = {"bvh": BVH, "bvh2": BVH2, "brute": BRUTE}[wl.hitter]
     P.material = _material(wl.material)
     P.force_rand = -1.0 if wl.force_rand is None else float(wl.force_rand)
     P.flags = L.FLAG_REF_QUIRKS if wl.quirks else 0
@@ -271,7 +272,7 @@ class TraceStep:
     def __init__(self, wl, scene: Optional[Scene] = None, ray_begin: int = 0, ray_end: int = 0):
         torch = _torch()
         self.wl = wl
-        self.scene = scene if scene is not None else Scene(wl.tris, wl.first_diffuse, bvh=(wl.hitter == "bvh"))
+        self.scene = scene if scene is not None else Scene(wl.tris, wl.first_diffuse, bvh=(wl.hitter != "brute"))
         self.params = trace_params(wl, ray_begin, ray_end)
         n_grid = wl.n_rays
         re = n_grid if ray_end <= 0 or ray_end > n_grid else ray_end

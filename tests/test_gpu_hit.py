@@ -33,7 +33,7 @@ def test_brute_and_bvh_match_oracle(torch_cuda, subdiv, noise):
     rays = random_rays(4000, 11 + subdiv, tris.shape[0])
     o_hit, o_t = O.next_hit(rays, tris)
     assert (o_hit > 1).sum() > 1000, "test rays should mostly hit"
-    for hitter in (tracer.BRUTE, tracer.BVH):
+    for hitter in (tracer.BRUTE, tracer.BVH, tracer.BVH2):
         hit, t = _hits(tracer, scene, hitter, rays)
         assert np.array_equal(hit, o_hit), f"hitter {hitter}: {np.nonzero(hit != o_hit)[0][:10]}"
         assert np.array_equal(t.view(np.uint32), o_t.view(np.uint32)), f"hitter {hitter}: t bits differ"
@@ -62,9 +62,10 @@ def test_bvh_equals_brute_large_scene(torch_cuda):
     scene = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
     rays = random_rays(1 << 16, 3, wl.n_tris)
     hb, tb = _hits(tracer, scene, tracer.BRUTE, rays)
-    hv, tv = _hits(tracer, scene, tracer.BVH, rays)
-    assert np.array_equal(hb, hv)
-    assert np.array_equal(tb.view(np.uint32), tv.view(np.uint32))
+    for hitter in (tracer.BVH, tracer.BVH2):
+        hv, tv = _hits(tracer, scene, hitter, rays)
+        assert np.array_equal(hb, hv)
+        assert np.array_equal(tb.view(np.uint32), tv.view(np.uint32))
     sample = np.arange(0, 1 << 16, 97)
     o_hit, o_t = O.next_hit(rays[sample], wl.tris)
     assert np.array_equal(hb[sample], o_hit)
@@ -82,7 +83,7 @@ def test_edge_cases(torch_cuda):
     rays["dir"][2] = [0.0, -1.0, 0.0]  # axis-aligned
     rays["pos"][2] = [0.0, 5.0, 0.0]
     o_hit, o_t = O.next_hit(rays, tris)
-    for hitter in (tracer.BRUTE, tracer.BVH):
+    for hitter in (tracer.BRUTE, tracer.BVH, tracer.BVH2):
         hit, t = _hits(tracer, scene, hitter, rays)
         assert np.array_equal(hit, o_hit)
     assert o_hit[0] == 1 and o_hit[1] == 1 and o_hit[2] > 1
@@ -94,13 +95,13 @@ def test_edge_cases(torch_cuda):
     assert tracer.next_hit(scene, tracer.BRUTE, d).numel() == 0
     # a scene with only the sentinel: everything misses
     only = tracer.Scene(tris[:1], 2, bvh=True)
-    for hitter in (tracer.BRUTE, tracer.BVH):
+    for hitter in (tracer.BRUTE, tracer.BVH, tracer.BVH2):
         hit, t = _hits(tracer, only, hitter, rays)
         assert (hit == 1).all() and np.isinf(t).all()
     # one real triangle
     one = tracer.Scene(tris[:2], 3, bvh=True)
     o1, _ = O.next_hit(rays, tris[:2])
-    for hitter in (tracer.BRUTE, tracer.BVH):
+    for hitter in (tracer.BRUTE, tracer.BVH, tracer.BVH2):
         hit, _ = _hits(tracer, one, hitter, rays)
         assert np.array_equal(hit, o1)
     del empty
@@ -130,9 +131,33 @@ def test_degenerate_geometry_matches_oracle(torch_cuda):
     rays["ignore_tri"] = np.where(rng.uniform(size=n) < 0.5, rng.integers(2, tris.shape[0] + 1, size=n), 1)
     rays["status"] = T.STATUS_ACTIVE
     o_hit, o_t = O.next_hit(rays, tris)
-    for hitter in (tracer.BRUTE, tracer.BVH):
+    for hitter in (tracer.BRUTE, tracer.BVH, tracer.BVH2):
         hit, t = _hits(tracer, scene, hitter, rays)
         bad = np.nonzero(hit != o_hit)[0]
         assert bad.size == 0, f"hitter {hitter}: {bad[:10]} {hit[bad[:5]]} vs {o_hit[bad[:5]]}"
         assert np.array_equal(t.view(np.uint32), o_t.view(np.uint32))
     assert (o_hit > 1).mean() > 0.5
+
+
+def test_refit_after_geometry_change(torch_cuda):
+    """splat_scene_update with moved and deformed triangles: after the repack
+    and the bottom-up refit both BVHs still return the brute-force result."""
+    import torch
+
+    from splat_gb300 import tracer
+
+    tris, fd = small_scene(3, 0.05)
+    scene = tracer.Scene(tris, fd, bvh=True)
+    moved = tris.copy()
+    rng = np.random.default_rng(5)
+    moved[1:fd - 1, 1:4] += np.float32(0.3)  # translate the sphere ...
+    moved[1:fd - 1, 1:4] *= (1 + 0.05 * rng.uniform(-1, 1, size=(fd - 2, 3, 1))).astype(np.float32)  # ... and jitter it
+    a, b = moved[:, 1] - moved[:, 2], moved[:, 2] - moved[:, 3]
+    moved[:, 0] = np.cross(a, b)
+    scene.update(torch.from_numpy(moved.reshape(-1)).cuda())
+    rays = random_rays(5000, 8, tris.shape[0])
+    o_hit, o_t = O.next_hit(rays, moved)
+    for hitter in (tracer.BRUTE, tracer.BVH, tracer.BVH2):
+        hit, t = _hits(tracer, scene, hitter, rays)
+        assert np.array_equal(hit, o_hit), f"hitter {hitter}"
+        assert np.array_equal(t.view(np.uint32), o_t.view(np.uint32))

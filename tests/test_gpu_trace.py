@@ -102,8 +102,9 @@ def test_realtime_full_size_properties(torch_cuda):
     a, sa = _gpu(wl, scene=scene)
     b, sb = _gpu(wl, scene=scene)
     assert np.array_equal(a, b) and sa == sb
-    c, sc = _gpu(wl.with_(hitter="brute"), scene=scene)
-    assert np.array_equal(a, c) and sa["rays_per_bounce"] == sc["rays_per_bounce"]
+    for other in ("brute", "bvh2"):
+        c, sc = _gpu(wl.with_(hitter=other), scene=scene)
+        assert np.array_equal(a, c) and sa["rays_per_bounce"] == sc["rays_per_bounce"]
     n = wl.n_rays
     cuts = [0, n // 3, n // 2 + 17, n]
     parts = sum(_gpu(wl, lo, hi, scene=scene)[0].astype(np.int64) for lo, hi in zip(cuts[:-1], cuts[1:]))
