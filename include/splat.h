@@ -268,6 +268,56 @@ splat_status_t splat_trace_forward_host(splat_scene_t* scene, const splat_ftri_t
                                         void* d_workspace, size_t workspace_bytes, splat_trace_stats_t* host_stats,
                                         void* stream);
 
+/* ----------------------------------------------------------- batch engine */
+/* Many frames of many scenes traced together (the batched and served
+ * forms).  An item is one frame: a resident scene, its trace parameters and
+ * its light map.  splat_batch_tick advances every in-flight item by one
+ * bounce in one launch sequence; an item admitted between ticks starts at the
+ * next tick, so requests join and leave at bounce granularity while others
+ * are in flight (continuous batching).  Draws are keyed by the item's seed
+ * and each ray's grid index and int32 maps add exactly, so an item's map is
+ * the one splat_trace_forward produces, alone or in any mix.
+ * The pool holds max_pool_rays rays of items in flight (library-owned device
+ * memory, splat_batch_device_bytes).  Items keep pointers into their scene:
+ * a scene must outlive its items.  BVH2 items use the four-wide BVH. */
+typedef struct splat_batch splat_batch_t;
+size_t splat_batch_device_bytes(int32_t max_items, int64_t max_pool_rays);
+splat_status_t splat_batch_create(int32_t max_items, int64_t max_pool_rays, splat_batch_t** out);
+splat_status_t splat_batch_destroy(splat_batch_t* batch);
+/* Admits one frame; SPLAT_ERR_WORKSPACE when no slot or pool room is free
+ * (retry after a tick).  The map is cleared at the item's first tick when
+ * params->zero_map is set. */
+splat_status_t splat_batch_admit(splat_batch_t* batch, const splat_scene_t* scene,
+                                 const splat_trace_params_t* params, void* d_map, int32_t* slot);
+/* Enqueues one tick on the stream.  done_slots receives the items whose last
+ * bounce runs in this tick: their maps are complete once the stream reaches
+ * this point. */
+splat_status_t splat_batch_tick(splat_batch_t* batch, void* stream, int32_t* done_slots, int32_t max_done,
+                                int32_t* n_done);
+/* Frees a completed item's slot. */
+splat_status_t splat_batch_release(splat_batch_t* batch, int32_t slot);
+splat_status_t splat_batch_status(const splat_batch_t* batch, int32_t* in_flight, int64_t* pool_rays, int32_t* tick);
+/* Captures the ticks that run every admitted item to completion into a CUDA
+ * graph (all items must start at the current tick; the stream must be a
+ * created stream, not a default one).  splat_batch_replay
+ * launches it again, optionally with new per-slot seeds. */
+splat_status_t splat_batch_capture(splat_batch_t* batch, void* stream, int32_t* n_ticks);
+splat_status_t splat_batch_replay(splat_batch_t* batch, const uint64_t* seeds, int32_t n_seeds, void* stream);
+
+/* ---------------------------------------------------------------- tuning */
+/* Launch-shape knobs (blocks per SM of the grid-stride kernels, process-wide).
+ * They change only how work is spread over the GPU, never a result; the
+ * autotuner (splat_gb300/autotune.py) picks them per workload. */
+enum {
+    SPLAT_TUNE_BRUTE_BLOCKS_PER_SM = 0, /* brute force: triangle-range splits target (default 4) */
+    SPLAT_TUNE_BVH_BLOCKS_PER_SM = 1,   /* BVH traversal grid (default 16) */
+    SPLAT_TUNE_EVOLVE_BLOCKS_PER_SM = 2, /* evolve grid (default 8) */
+    SPLAT_TUNE_SPLAT_BLOCKS_PER_SM = 3,  /* splat grid (default 8) */
+    SPLAT_TUNE_KEYS = 4
+};
+splat_status_t splat_set_tuning(int32_t key, int32_t value);
+int32_t splat_get_tuning(int32_t key);
+
 /* ------------------------------------------------------------- profiling */
 /* Launch profiling: while a profile is attached to the calling thread, every
  * kernel libsplat launches from that thread is bracketed by CUDA events on
@@ -280,7 +330,8 @@ enum {
     SPLAT_KERNEL_EVOLVE = 3,
     SPLAT_KERNEL_AUX = 4, /* fills, unpacks, conversions, stats, refit, packing */
     SPLAT_KERNEL_SPLAT = 5,
-    SPLAT_KERNEL_KINDS = 6
+    SPLAT_KERNEL_BATCH = 6, /* one whole batch tick */
+    SPLAT_KERNEL_KINDS = 7
 };
 typedef struct splat_profile splat_profile_t;
 splat_status_t splat_profile_create(int32_t max_launches, splat_profile_t** out);

@@ -94,6 +94,17 @@ SIGNATURES = {
     "splat_trace_workspace_size": ([i64], sz),
     "splat_trace_forward": ([vp, C.POINTER(TraceParams), vp, vp, sz, vp, vp], i32),
     "splat_trace_forward_host": ([vp, vp, C.POINTER(TraceParams), vp, vp, vp, sz, C.POINTER(TraceStats), vp], i32),
+    "splat_batch_device_bytes": ([i32, i64], sz),
+    "splat_batch_create": ([i32, i64, vp], i32),
+    "splat_batch_destroy": ([vp], i32),
+    "splat_batch_admit": ([vp, vp, C.POINTER(TraceParams), vp, C.POINTER(C.c_int32)], i32),
+    "splat_batch_tick": ([vp, vp, vp, i32, C.POINTER(C.c_int32)], i32),
+    "splat_batch_release": ([vp, i32], i32),
+    "splat_batch_status": ([vp, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int32)], i32),
+    "splat_batch_capture": ([vp, vp, C.POINTER(C.c_int32)], i32),
+    "splat_batch_replay": ([vp, vp, i32, vp], i32),
+    "splat_set_tuning": ([i32, i32], i32),
+    "splat_get_tuning": ([i32], i32),
     "splat_profile_create": ([i32, vp], i32),
     "splat_profile_attach": ([vp], i32),
     "splat_profile_read": ([vp, i32, C.POINTER(C.c_int64), C.POINTER(C.c_double)], i32),
@@ -101,13 +112,19 @@ SIGNATURES = {
     "splat_profile_destroy": ([vp], i32),
 }
 
+TUNE_BRUTE_BLOCKS_PER_SM = 0
+TUNE_BVH_BLOCKS_PER_SM = 1
+TUNE_EVOLVE_BLOCKS_PER_SM = 2
+TUNE_SPLAT_BLOCKS_PER_SM = 3
+
 KERNEL_GENERATE = 0
 KERNEL_HIT_BRUTE = 1
 KERNEL_HIT_BVH = 2
 KERNEL_EVOLVE = 3
 KERNEL_AUX = 4
 KERNEL_SPLAT = 5
-KERNEL_ALL = 6
+KERNEL_BATCH = 6
+KERNEL_ALL = 7
 
 _lib = None
 _lock = threading.Lock()

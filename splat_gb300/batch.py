@@ -1,0 +1,111 @@
+"""Batched and served forms: many frames of many scenes in one launch
+sequence (libsplat's batch engine, include/splat.h splat_batch_*).
+
+Batch.admit queues a frame (scene + workload parameters + light map);
+Batch.tick advances every in-flight frame by one bounce; frames admitted
+between ticks join at the next tick.  capture() / replay() turn a fixed set of
+admitted frames into one CUDA graph.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Optional, Sequence
+
+from . import _lib as L
+from . import tracer
+
+
+class PoolFull(RuntimeError):
+    """No slot or pool room for the frame right now; retry after a tick."""
+
+
+class Batch:
+    def __init__(self, max_items: int, max_pool_rays: int):
+        lib = L.load()
+        h = C.c_void_p()
+        L.check(lib.splat_batch_create(int(max_items), int(max_pool_rays), C.byref(h)))
+        self._h = h
+        self.max_items = int(max_items)
+        self.max_pool_rays = int(max_pool_rays)
+        self._done = (C.c_int32 * self.max_items)()
+        self.items = {}
+
+    @staticmethod
+    def device_bytes(max_items: int, max_pool_rays: int) -> int:
+        return int(L.load().splat_batch_device_bytes(int(max_items), int(max_pool_rays)))
+
+    def admit(self, scene: "tracer.Scene", wl, tex, seed: Optional[int] = None, ray_begin: int = 0,
+              ray_end: int = 0) -> int:
+        P = tracer.trace_params(wl, ray_begin, ray_end)
+        if seed is not None:
+            P.seed = int(seed)
+        slot = C.c_int32(-1)
+        rc = L.load().splat_batch_admit(self._h, scene.handle, C.byref(P), tex.data_ptr(), C.byref(slot))
+        if rc == L.ERR_WORKSPACE:
+            raise PoolFull(L.load().splat_last_error().decode())
+        L.check(rc)
+        self.items[slot.value] = (scene, wl, tex)
+        return slot.value
+
+    def tick(self, stream: Optional[int] = None) -> List[int]:
+        n = C.c_int32(0)
+        st = tracer._stream() if stream is None else stream
+        L.check(L.load().splat_batch_tick(self._h, st, self._done, self.max_items, C.byref(n)))
+        return [self._done[i] for i in range(n.value)]
+
+    def release(self, slot: int) -> None:
+        L.check(L.load().splat_batch_release(self._h, int(slot)))
+        self.items.pop(slot, None)
+
+    def status(self):
+        f, r, t = C.c_int32(), C.c_int64(), C.c_int32()
+        L.check(L.load().splat_batch_status(self._h, C.byref(f), C.byref(r), C.byref(t)))
+        return {"in_flight": f.value, "pool_rays": r.value, "tick": t.value}
+
+    def run(self) -> List[int]:
+        """Ticks until nothing is in flight; returns slots in completion order."""
+        done = []
+        while self.status()["in_flight"] > 0:
+            done += self.tick()
+        return done
+
+    def _graph_stream(self):
+        """Capture and replay run on a stream of their own (the default stream
+        cannot be captured), ordered after and before the current stream."""
+        import torch
+
+        if getattr(self, "_gs", None) is None:
+            self._gs = torch.cuda.Stream()
+        self._gs.wait_stream(torch.cuda.current_stream())
+        return self._gs
+
+    def capture(self) -> int:
+        import torch
+
+        n = C.c_int32(0)
+        gs = self._graph_stream()
+        L.check(L.load().splat_batch_capture(self._h, gs.cuda_stream, C.byref(n)))
+        torch.cuda.current_stream().wait_stream(gs)
+        return n.value
+
+    def replay(self, seeds: Optional[Sequence[int]] = None) -> None:
+        import torch
+
+        gs = self._graph_stream()
+        if seeds:
+            arr = (C.c_uint64 * len(seeds))(*[int(x) for x in seeds])
+            L.check(L.load().splat_batch_replay(self._h, arr, len(seeds), gs.cuda_stream))
+        else:
+            L.check(L.load().splat_batch_replay(self._h, None, 0, gs.cuda_stream))
+        torch.cuda.current_stream().wait_stream(gs)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            L.load().splat_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

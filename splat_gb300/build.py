@@ -19,9 +19,9 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsplat.so")
 ROOT = os.path.dirname(HERE)
 
-CU_SOURCES = ["api.cu", "hit.cu", "evolve.cu"]
+CU_SOURCES = ["api.cu", "hit.cu", "evolve.cu", "batch.cu"]
 CPP_SOURCES = ["bvh_build.cpp"]
-HEADERS = ["common.cuh", "optics.cuh", "kernels.h", "bvh_build.h"]
+HEADERS = ["common.cuh", "optics.cuh", "kernels.h", "bvh_build.h", "hitcore.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [

@@ -685,6 +685,15 @@ splat_status_t splat_trace_forward_host(splat_scene_t* scene, const splat_ftri_t
     return SPLAT_OK;
 }
 
+splat_status_t splat_set_tuning(int32_t key, int32_t value) {
+    if (key < 0 || key >= SPLAT_TUNE_KEYS) return fail(SPLAT_ERR_INVALID, "set_tuning: unknown key");
+    if (value < 1 || value > 256) return fail(SPLAT_ERR_INVALID, "set_tuning: value must be 1..256");
+    g_tune[key] = value;
+    return SPLAT_OK;
+}
+
+int32_t splat_get_tuning(int32_t key) { return key < 0 || key >= SPLAT_TUNE_KEYS ? -1 : g_tune[key]; }
+
 splat_status_t splat_profile_create(int32_t max_launches, splat_profile_t** out) {
     if (!out || max_launches < 1 || max_launches > (1 << 20)) return fail(SPLAT_ERR_INVALID, "profile_create: bad argument");
     splat_profile* p = new (std::nothrow) splat_profile();
@@ -739,6 +748,350 @@ splat_status_t splat_profile_destroy(splat_profile_t* p) {
     if (g_prof == p) g_prof = nullptr;
     for (auto& e : p->ev) cudaEventDestroy(e);
     delete p;
+    return SPLAT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// batch engine
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct splat_batch {
+    int device = 0;
+    int32_t max_items = 0;
+    int64_t cap = 0;
+    size_t item_bytes = 0;
+    char* d_mem = nullptr;
+    size_t d_bytes = 0;
+    void* d_items = nullptr;
+    void* d_fresh = nullptr;
+    RaySoA a{}, b{}, q{};
+    int32_t* hit = nullptr;
+    int64_t* counts = nullptr;  // [0], [1]: ping-pong active counts, [2]: splat queue
+    int32_t* d_err = nullptr;
+    char* h_stage[2] = {nullptr, nullptr};  // pinned copies of the item table
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+    int stage_idx = 0;
+    std::vector<char> h_items;
+    std::vector<uint8_t> used;
+    std::vector<int64_t> rays;
+    std::vector<int32_t> start, depth;
+    std::vector<void*> maps;
+    std::vector<size_t> map_bytes;
+    std::vector<uint8_t> zero_map;
+    int32_t tick = 0;
+    int parity = 0;
+    bool dirty = true;
+    cudaGraphExec_t exec = nullptr;
+    int32_t cap_t1 = 0;      // host tick after the captured ticks
+    int cap_parity1 = 0;     // buffer parity after them
+};
+
+namespace {
+
+size_t batch_bytes(int32_t max_items, int64_t cap) {
+    return align_up(batch_item_bytes() * (size_t)max_items) + align_up(batch_fresh_bytes()) + 3 * soa_bytes(cap) +
+           align_up(4 * (size_t)cap) + kCounterBytes + kAlign;
+}
+
+void batch_free(splat_batch* b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    cudaFree(b->d_mem);
+    for (int i = 0; i < 2; ++i) {
+        if (b->h_stage[i]) cudaFreeHost(b->h_stage[i]);
+        if (b->stage_ev[i]) cudaEventDestroy(b->stage_ev[i]);
+    }
+    delete b;
+}
+
+// Pool rays still needed by items whose last tick is at or after `tick`.
+int64_t pool_in_use(const splat_batch* b) {
+    int64_t r = 0;
+    for (int32_t s = 0; s < b->max_items; ++s)
+        if (b->used[(size_t)s] && b->start[(size_t)s] + b->depth[(size_t)s] - 1 >= b->tick) r += b->rays[(size_t)s];
+    return r;
+}
+
+splat_status_t batch_upload(splat_batch* b, cudaStream_t st) {
+    if (!b->dirty) return SPLAT_OK;
+    const int i = b->stage_idx;
+    b->stage_idx ^= 1;
+    SPLAT_CUDA(cudaEventSynchronize(b->stage_ev[i]), "batch: stage reuse");
+    std::memcpy(b->h_stage[i], b->h_items.data(), b->h_items.size());
+    SPLAT_CUDA(cudaMemcpyAsync(b->d_items, b->h_stage[i], b->h_items.size(), cudaMemcpyHostToDevice, st),
+               "batch: upload items");
+    SPLAT_CUDA(cudaEventRecord(b->stage_ev[i], st), "batch: stage event");
+    b->dirty = false;
+    return SPLAT_OK;
+}
+
+// Enqueues one tick (no table upload).
+splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done_slots, int32_t max_done,
+                                  int32_t* n_done) {
+    int64_t fresh_rays = 0, cap_rays = 0;
+    int32_t nd = 0;
+    for (int32_t s = 0; s < b->max_items; ++s) {
+        if (!b->used[(size_t)s]) continue;
+        const int32_t st0 = b->start[(size_t)s], last = st0 + b->depth[(size_t)s] - 1;
+        if (b->tick < st0 || b->tick > last) continue;
+        cap_rays += b->rays[(size_t)s];
+        if (b->tick == st0) {
+            fresh_rays += b->rays[(size_t)s];
+            if (b->zero_map[(size_t)s])
+                SPLAT_CUDA(cudaMemsetAsync(b->maps[(size_t)s], 0, b->map_bytes[(size_t)s], st), "batch: clear map");
+        }
+        if (b->tick == last) {
+            if (done_slots && nd < max_done) done_slots[nd] = s;
+            ++nd;
+        }
+    }
+    if (n_done) *n_done = nd;
+    int64_t* cur_count = &b->counts[b->parity];
+    int64_t* next_count = &b->counts[b->parity ^ 1];
+    SPLAT_CUDA(cudaMemsetAsync(next_count, 0, sizeof(int64_t), st), "batch: reset count");
+    SPLAT_CUDA(cudaMemsetAsync(&b->counts[2], 0, sizeof(int64_t), st), "batch: reset queue");
+    if (cap_rays > 0) {
+        ProfScope ps(SPLAT_KERNEL_BATCH, st);
+        BatchTickArgs a;
+        a.items = b->d_items;
+        a.n_slots = b->max_items;
+        a.tick = b->tick;
+        a.fresh = b->d_fresh;
+        a.cur = b->parity ? b->b : b->a;
+        a.next = b->parity ? b->a : b->b;
+        a.queue = b->q;
+        a.cur_count = cur_count;
+        a.next_count = next_count;
+        a.queue_count = &b->counts[2];
+        a.fresh_rays = fresh_rays;
+        a.cap_rays = cap_rays;
+        a.hit_idx = b->hit;
+        a.err = b->d_err;
+        a.sm_count = sm_count_current();
+        SPLAT_CUDA(launch_batch_tick(a, st), "batch tick");
+        b->parity ^= 1;
+    }
+    b->tick += 1;
+    return SPLAT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t splat_batch_device_bytes(int32_t max_items, int64_t max_pool_rays) {
+    return max_items < 1 || max_pool_rays < 1 ? 0 : batch_bytes(max_items, max_pool_rays);
+}
+
+splat_status_t splat_batch_create(int32_t max_items, int64_t max_pool_rays, splat_batch_t** out) {
+    if (!out) return fail(SPLAT_ERR_INVALID, "batch_create: out is null");
+    *out = nullptr;
+    if (max_items < 1 || max_items > 256) return fail(SPLAT_ERR_INVALID, "batch_create: max_items must be 1..256");
+    if (max_pool_rays < 1 || max_pool_rays > (int64_t(1) << 31))
+        return fail(SPLAT_ERR_INVALID, "batch_create: max_pool_rays must be 1..2^31");
+    splat_batch* b = new (std::nothrow) splat_batch();
+    if (!b) return fail(SPLAT_ERR_ALLOC, "batch_create: host allocation");
+    cudaGetDevice(&b->device);
+    b->max_items = max_items;
+    b->cap = max_pool_rays;
+    b->item_bytes = batch_item_bytes();
+    b->d_bytes = batch_bytes(max_items, max_pool_rays);
+    cudaError_t e = cudaMalloc(&b->d_mem, b->d_bytes);
+    if (e != cudaSuccess) {
+        delete b;
+        return fail(SPLAT_ERR_ALLOC, std::string("batch_create: cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    char* p = reinterpret_cast<char*>(align_up(reinterpret_cast<size_t>(b->d_mem)));
+    b->d_items = p;
+    p += align_up(b->item_bytes * (size_t)max_items);
+    b->d_fresh = p;
+    p += align_up(batch_fresh_bytes());
+    b->a = carve_soa(p, max_pool_rays);
+    b->b = carve_soa(p, max_pool_rays);
+    b->q = carve_soa(p, max_pool_rays);
+    b->hit = reinterpret_cast<int32_t*>(p);
+    p += align_up(4 * (size_t)max_pool_rays);
+    b->counts = reinterpret_cast<int64_t*>(p);
+    b->d_err = reinterpret_cast<int32_t*>(p + 512);
+    const size_t table = b->item_bytes * (size_t)max_items;
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+        e = cudaMallocHost(&b->h_stage[i], table);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->stage_ev[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaMemset(b->counts, 0, kCounterBytes);
+    if (e != cudaSuccess) {
+        batch_free(b);
+        return fail(SPLAT_ERR_ALLOC, std::string("batch_create: ") + cudaGetErrorString(e));
+    }
+    b->h_items.assign(table, 0);
+    for (int32_t s = 0; s < max_items; ++s) batch_clear_item(b->h_items.data() + b->item_bytes * (size_t)s);
+    b->used.assign((size_t)max_items, 0);
+    b->rays.assign((size_t)max_items, 0);
+    b->start.assign((size_t)max_items, -1);
+    b->depth.assign((size_t)max_items, 0);
+    b->maps.assign((size_t)max_items, nullptr);
+    b->map_bytes.assign((size_t)max_items, 0);
+    b->zero_map.assign((size_t)max_items, 0);
+    *out = b;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_batch_destroy(splat_batch_t* b) {
+    if (!b) return fail(SPLAT_ERR_INVALID, "batch_destroy: null batch");
+    cudaDeviceSynchronize();
+    batch_free(b);
+    return SPLAT_OK;
+}
+
+splat_status_t splat_batch_admit(splat_batch_t* b, const splat_scene_t* scene, const splat_trace_params_t* P,
+                                 void* d_map, int32_t* slot_out) {
+    if (!b || !scene || !P || !slot_out) return fail(SPLAT_ERR_INVALID, "batch_admit: null argument");
+    *slot_out = -1;
+    if (!light_ok(&P->light, P->upscale)) return fail(SPLAT_ERR_INVALID, "batch_admit: bad light / upscale");
+    if (P->depth < 1 || P->depth > 8) return fail(SPLAT_ERR_INVALID, "batch_admit: depth must be 1..8");
+    if (!valid_material(&P->material)) return fail(SPLAT_ERR_INVALID, "batch_admit: bad material");
+    if (P->lambda_mode.mode == SPLAT_LAMBDA_STRATIFIED && P->lambda_mode.n_strata < 1)
+        return fail(SPLAT_ERR_INVALID, "batch_admit: n_strata < 1");
+    splat_status_t rc =
+        check_map(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
+    if (rc != SPLAT_OK) return rc;
+    const bool bvh = P->hitter == SPLAT_HITTER_BVH || P->hitter == SPLAT_HITTER_BVH2;
+    if (bvh && !scene->d_nodes4 && scene->n_recs > 0)
+        return fail(SPLAT_ERR_INVALID, "batch_admit: BVH hitter on a scene without BVH");
+    const int64_t n_grid = grid_rays(P);
+    const int64_t rb = P->ray_begin < 0 ? 0 : P->ray_begin;
+    const int64_t re = (P->ray_end <= 0 || P->ray_end > n_grid) ? n_grid : P->ray_end;
+    const int64_t n = re - rb;
+    if (n <= 0) return fail(SPLAT_ERR_INVALID, "batch_admit: empty ray range");
+    if (n > (int64_t(1) << 24)) return fail(SPLAT_ERR_INVALID, "batch_admit: more than 2^24 rays in one item");
+    if (n_grid >= (int64_t(1) << 32)) return fail(SPLAT_ERR_INVALID, "batch_admit: more than 2^32 grid rays");
+    int32_t slot = -1;
+    for (int32_t s = 0; s < b->max_items; ++s)
+        if (!b->used[(size_t)s]) {
+            slot = s;
+            break;
+        }
+    if (slot < 0) return fail(SPLAT_ERR_WORKSPACE, "batch_admit: no free slot");
+    if (pool_in_use(b) + n > b->cap) return fail(SPLAT_ERR_WORKSPACE, "batch_admit: ray pool full");
+    GenParams g;
+    g.light = P->light;
+    g.upscale = P->upscale;
+    g.lm = P->lambda_mode;
+    g.seed = P->seed;
+    g.light_index = 0;
+    g.ray_begin = rb;
+    BatchSceneRef sc{scene->d_ftri, scene->d_brute, scene->d_nodes4, scene->d_bvh, scene->n_recs, scene->n_tris,
+                     scene->first_diffuse};
+    const SplatParams sp =
+        make_splat(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
+    batch_fill_item(b->h_items.data() + b->item_bytes * (size_t)slot, sc, g, n, P->depth,
+                    bvh ? SPLAT_HITTER_BVH : SPLAT_HITTER_BRUTE, b->tick, (P->flags & SPLAT_FLAG_REF_QUIRKS) ? 1 : 0,
+                    P->force_rand, P->material, sp);
+    b->used[(size_t)slot] = 1;
+    b->rays[(size_t)slot] = n;
+    b->start[(size_t)slot] = b->tick;
+    b->depth[(size_t)slot] = P->depth;
+    b->maps[(size_t)slot] = d_map;
+    b->map_bytes[(size_t)slot] = (size_t)P->map_w * P->map_h * (P->n_lambda > 0 ? P->n_lambda : 1) * 4;
+    b->zero_map[(size_t)slot] = P->zero_map ? 1 : 0;
+    b->dirty = true;
+    *slot_out = slot;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_batch_tick(splat_batch_t* b, void* stream, int32_t* done_slots, int32_t max_done,
+                                int32_t* n_done) {
+    if (!b) return fail(SPLAT_ERR_INVALID, "batch_tick: null batch");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    splat_status_t rc = batch_upload(b, st);
+    if (rc != SPLAT_OK) return rc;
+    return batch_enqueue_tick(b, st, done_slots, max_done, n_done);
+}
+
+splat_status_t splat_batch_release(splat_batch_t* b, int32_t slot) {
+    if (!b || slot < 0 || slot >= b->max_items || !b->used[(size_t)slot])
+        return fail(SPLAT_ERR_INVALID, "batch_release: bad slot");
+    if (b->start[(size_t)slot] + b->depth[(size_t)slot] - 1 >= b->tick)
+        return fail(SPLAT_ERR_INVALID, "batch_release: item still in flight");
+    b->used[(size_t)slot] = 0;
+    b->start[(size_t)slot] = -1;
+    batch_clear_item(b->h_items.data() + b->item_bytes * (size_t)slot);
+    b->dirty = true;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_batch_status(const splat_batch_t* b, int32_t* in_flight, int64_t* pool_rays, int32_t* tick) {
+    if (!b) return fail(SPLAT_ERR_INVALID, "batch_status: null batch");
+    int32_t f = 0;
+    for (int32_t s = 0; s < b->max_items; ++s)
+        if (b->used[(size_t)s] && b->start[(size_t)s] + b->depth[(size_t)s] - 1 >= b->tick) ++f;
+    if (in_flight) *in_flight = f;
+    if (pool_rays) *pool_rays = pool_in_use(b);
+    if (tick) *tick = b->tick;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_batch_capture(splat_batch_t* b, void* stream, int32_t* n_ticks) {
+    if (!b) return fail(SPLAT_ERR_INVALID, "batch_capture: null batch");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    int32_t last = b->tick - 1;
+    for (int32_t s = 0; s < b->max_items; ++s) {
+        if (!b->used[(size_t)s] || b->start[(size_t)s] + b->depth[(size_t)s] - 1 < b->tick) continue;
+        if (b->start[(size_t)s] != b->tick)
+            return fail(SPLAT_ERR_INVALID, "batch_capture: an item is already in flight");
+        last = std::max(last, b->start[(size_t)s] + b->depth[(size_t)s] - 1);
+    }
+    if (last < b->tick) return fail(SPLAT_ERR_INVALID, "batch_capture: no admitted item");
+    if (st == nullptr || st == cudaStreamLegacy || st == cudaStreamPerThread)
+        return fail(SPLAT_ERR_INVALID, "batch_capture: needs a created (non-default) stream");
+    splat_status_t rc = batch_upload(b, st);
+    if (rc != SPLAT_OK) return rc;
+    SPLAT_CUDA(cudaStreamSynchronize(st), "batch_capture: sync");
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    const int32_t t0 = b->tick;
+    const int p0 = b->parity;
+    cudaGraph_t graph = nullptr;
+    SPLAT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "batch_capture: begin");
+    cudaError_t e = cudaMemsetAsync(&b->counts[p0], 0, sizeof(int64_t), st);
+    rc = SPLAT_OK;
+    while (e == cudaSuccess && rc == SPLAT_OK && b->tick <= last) rc = batch_enqueue_tick(b, st, nullptr, 0, nullptr);
+    cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess) return cuda_fail(e, "batch_capture: memset");
+    if (rc != SPLAT_OK) return rc;
+    if (e2 != cudaSuccess) return cuda_fail(e2, "batch_capture: end");
+    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "batch_capture: instantiate");
+    if (n_ticks) *n_ticks = b->tick - t0;
+    // the captured ticks have not run yet: each replay runs them
+    b->cap_t1 = b->tick;
+    b->cap_parity1 = b->parity;
+    b->tick = t0;
+    b->parity = p0;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_batch_replay(splat_batch_t* b, const uint64_t* seeds, int32_t n_seeds, void* stream) {
+    if (!b || !b->exec) return fail(SPLAT_ERR_INVALID, "batch_replay: nothing captured");
+    if (n_seeds < 0 || n_seeds > b->max_items || (n_seeds > 0 && !seeds))
+        return fail(SPLAT_ERR_INVALID, "batch_replay: bad seeds");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    for (int32_t s = 0; s < n_seeds; ++s) {
+        batch_set_seed(b->h_items.data() + b->item_bytes * (size_t)s, seeds[s]);
+        b->dirty = true;
+    }
+    splat_status_t rc = batch_upload(b, st);
+    if (rc != SPLAT_OK) return rc;
+    ProfScope ps(SPLAT_KERNEL_BATCH, st);
+    SPLAT_CUDA(cudaGraphLaunch(b->exec, st), "batch_replay: launch");
+    if (b->tick < b->cap_t1) {
+        b->tick = b->cap_t1;
+        b->parity = b->cap_parity1;
+    }
     return SPLAT_OK;
 }
 

@@ -1,0 +1,267 @@
+// batch.cu -- many frames of many scenes traced together.
+//
+// An item is one frame: a resident scene plus one splat_trace_params_t and
+// its light map.  Items live in a device table; their rays share one
+// structure-of-arrays pool whose ray ids carry the item slot (slot << 24 |
+// local ray index).  One tick advances every in-flight item by one bounce:
+//
+//   reserve   one thread appends the rays of items starting this tick after
+//             the survivors of the previous tick
+//   generate  rays_from_light of those items (src/ray_generators.jl:64-97)
+//   hit       per ray, its item's four-wide BVH or a per-ray brute loop
+//   evolve    per ray, evolve_ray with its item's material, seed and bounce
+//             (src/tracer.jl:181-201); compaction and the diffuse-ray queue
+//             as in the single-scene step
+//   splat     per queued ray (all its planes), into its item's light map
+//
+// Items therefore join and leave at bounce granularity: a request that
+// arrives while others are in flight starts at the next tick and overlaps
+// with them on the device (continuous batching).  Every draw is keyed by the
+// item's seed and the ray's grid index, and int32 maps accumulate exactly, so
+// an item's map is the same alone, in any mix, and through
+// splat_trace_forward.  A fixed set of admitted items can be captured once
+// into a CUDA graph and replayed (the batched form).
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "hitcore.cuh"
+#include "optics.cuh"
+
+namespace splat {
+
+constexpr int kSlotShift = 24;
+constexpr uint32_t kLocalMask = (1u << kSlotShift) - 1u;
+constexpr int kMaxBatchItems = 256;
+
+struct BatchItem {
+    const splat_ftri_t* ftri;
+    const TriHit* brute;
+    const Bvh4Node* nodes4;
+    const TriHit* bvh_tris;
+    int64_t n_recs, n_tris, first_diffuse;
+    int32_t hitter;      // SPLAT_HITTER_BRUTE or SPLAT_HITTER_BVH
+    int32_t depth;
+    int32_t start_tick;  // tick of the first bounce; < 0: slot unused
+    int32_t quirks;
+    float force_rand;
+    int32_t _pad0;
+    GenParams gen;
+    int64_t n_rays;
+    splat_material_t material;
+    SplatParams sp;
+};
+
+struct FreshList {
+    int32_t n;
+    int32_t _pad;
+    int64_t total;
+    int32_t slot[kMaxBatchItems];
+    int64_t prefix[kMaxBatchItems + 1];
+    int64_t offset[kMaxBatchItems];
+};
+
+__global__ void batch_reserve_kernel(const BatchItem* items, int n_slots, int tick, int64_t* cur_count,
+                                     FreshList* fresh) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    int f = 0;
+    int64_t run = 0;
+    const int64_t base = *cur_count;
+    for (int s = 0; s < n_slots; ++s) {
+        if (items[s].start_tick != tick) continue;
+        fresh->slot[f] = s;
+        fresh->prefix[f] = run;
+        fresh->offset[f] = base + run;
+        run += items[s].n_rays;
+        ++f;
+    }
+    fresh->prefix[f] = run;
+    fresh->n = f;
+    fresh->total = run;
+    *cur_count = base + run;
+}
+
+__global__ void batch_generate_kernel(const BatchItem* __restrict__ items, const FreshList* __restrict__ fresh,
+                                      RaySoA out) {
+    const int64_t total = fresh->total;
+    const int nf = fresh->n;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nf - 1;
+        while (lo < hi) {  // last f with prefix[f] <= g
+            const int mid = (lo + hi + 1) >> 1;
+            if (fresh->prefix[mid] <= g) lo = mid;
+            else hi = mid - 1;
+        }
+        const int slot = fresh->slot[lo];
+        const int64_t local = g - fresh->prefix[lo];
+        const BatchItem& it = items[slot];
+        const RayState r = gen_ray(it.gen, it.gen.ray_begin + local);
+        store_ray(out, fresh->offset[lo] + local, r, ((uint32_t)slot << kSlotShift) | (uint32_t)local);
+    }
+}
+
+__global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t* __restrict__ count,
+                                                        const BatchItem* __restrict__ items, int32_t* hit_idx,
+                                                        int32_t* err) {
+    const int64_t n = *count;
+    int stack_ref[kBvhStack];
+    float stack_t[kBvhStack];
+    RaySrc src{};
+    src.f = in.f;
+    src.ignore = in.ignore;
+    src.cap = in.cap;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const HitRay r = load_hit_ray<false>(src, k);
+        const BatchItem& it = items[in.id[k] >> kSlotShift];
+        float best;
+        int32_t bi;
+        if (it.hitter == SPLAT_HITTER_BVH && it.nodes4)
+            bvh4_closest(r, Bvh4View{it.nodes4, it.bvh_tris}, stack_ref, stack_t, err, best, bi);
+        else
+            brute_closest(r, it.brute, it.n_recs, best, bi);
+        hit_idx[k] = bi;
+    }
+}
+
+constexpr int kBatchThreads = 256;
+
+__global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, RaySoA out, RaySoA queue,
+                                                                     const int64_t* __restrict__ in_count,
+                                                                     int64_t* out_count, int64_t* queue_count,
+                                                                     const BatchItem* __restrict__ items, int tick,
+                                                                     const int32_t* __restrict__ hit_idx,
+                                                                     int32_t* err) {
+    __shared__ int s_keep[kBatchThreads / 32], s_dif[kBatchThreads / 32];
+    __shared__ unsigned long long s_kbase, s_dbase;
+    const int64_t n = *in_count;
+    const int lane = lane_id();
+    const int wid = threadIdx.x >> 5;
+    for (int64_t base = (int64_t)blockIdx.x * kBatchThreads; base < n; base += (int64_t)gridDim.x * kBatchThreads) {
+        const int64_t k = base + threadIdx.x;
+        bool keep = false, dif = false;
+        RayState o;
+        uint32_t id = 0;
+        if (k < n) {
+            const RayState r = load_ray(in, k);
+            id = in.id[k];
+            const BatchItem& it = items[id >> kSlotShift];
+            const uint32_t bounce = (uint32_t)(tick - it.start_tick + 1);
+            const EvolveView v{it.ftri, it.n_tris, err, it.first_diffuse, it.material, it.gen.seed, bounce,
+                               it.force_rand, it.quirks != 0, (int)bounce >= it.depth};
+            int32_t ih;
+            const uint32_t grid_id = (uint32_t)(it.gen.ray_begin + (id & kLocalMask));
+            const int fate = evolve_one<true>(r, hit_idx[k], grid_id, v, o, ih);
+            keep = fate == kFateKeep;
+            dif = fate == kFateDiffuse;
+        }
+        const unsigned kb = __ballot_sync(0xffffffffu, keep);
+        const unsigned db = __ballot_sync(0xffffffffu, dif);
+        if (lane == 0) {
+            s_keep[wid] = __popc(kb);
+            s_dif[wid] = __popc(db);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int tk = 0, td = 0;
+            for (int w = 0; w < kBatchThreads / 32; ++w) {
+                const int a = s_keep[w], b = s_dif[w];
+                s_keep[w] = tk;
+                s_dif[w] = td;
+                tk += a;
+                td += b;
+            }
+            s_kbase = tk ? atomicAdd(reinterpret_cast<unsigned long long*>(out_count), (unsigned long long)tk) : 0ull;
+            s_dbase = td ? atomicAdd(reinterpret_cast<unsigned long long*>(queue_count), (unsigned long long)td) : 0ull;
+        }
+        __syncthreads();
+        const unsigned below = (1u << lane) - 1u;
+        if (keep) store_ray(out, (int64_t)s_kbase + s_keep[wid] + __popc(kb & below), o, id);
+        else if (dif) store_ray(queue, (int64_t)s_dbase + s_dif[wid] + __popc(db & below), o, id);
+        __syncthreads();
+    }
+}
+
+// One lane per queued ray, walking all of its planes: rays of one item are
+// adjacent in the queue, so a warp's lanes usually share an item and its
+// plane count, and no lane idles on frames with few planes.
+__global__ void __launch_bounds__(256, 3) batch_splat_kernel(RaySoA q, const int64_t* __restrict__ count,
+                                                             const BatchItem* __restrict__ items) {
+    const int64_t n = *count;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const RayState r = load_ray(q, k);
+        const BatchItem& it = items[q.id[k] >> kSlotShift];
+        const int planes = it.sp.n_lambda > 0 ? it.sp.n_lambda : 1;
+        const Tri T = load_tri(it.ftri, r.ignore);
+        const TriUV quv = tri_uv(T);
+        for (int il = 0; il < planes; ++il) (void)splat_ray_plane(it.sp, r, T, quv, il);
+    }
+}
+
+static int grid_cap(int64_t n, int threads, int sm_count, int per_sm) {
+    int64_t b = (n + threads - 1) / threads;
+    const int64_t cap = (int64_t)sm_count * per_sm;
+    if (b > cap) b = cap;
+    return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s) {
+    const BatchItem* items = reinterpret_cast<const BatchItem*>(a.items);
+    FreshList* fresh = reinterpret_cast<FreshList*>(a.fresh);
+    batch_reserve_kernel<<<1, 32, 0, s>>>(items, a.n_slots, a.tick, a.cur_count, fresh);
+    ++g_launches;
+    if (a.fresh_rays > 0) {
+        batch_generate_kernel<<<grid_cap(a.fresh_rays, 256, a.sm_count, 8), 256, 0, s>>>(items, fresh, a.cur);
+        ++g_launches;
+    }
+    if (a.cap_rays > 0) {
+        batch_hit_kernel<<<grid_cap(a.cap_rays, 128, a.sm_count, 16), 128, 0, s>>>(a.cur, a.cur_count, items,
+                                                                                   a.hit_idx, a.err);
+        ++g_launches;
+        batch_evolve_kernel<<<grid_cap(a.cap_rays, kBatchThreads, a.sm_count, 8), kBatchThreads, 0, s>>>(
+            a.cur, a.next, a.queue, a.cur_count, a.next_count, a.queue_count, items, a.tick, a.hit_idx, a.err);
+        ++g_launches;
+        batch_splat_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count, items);
+        ++g_launches;
+    }
+    return cudaGetLastError();
+}
+
+size_t batch_item_bytes() { return sizeof(BatchItem); }
+size_t batch_fresh_bytes() { return sizeof(FreshList); }
+
+void batch_fill_item(void* dst, const BatchSceneRef& sc, const GenParams& gen, int64_t n_rays, int32_t depth,
+                     int32_t hitter, int32_t start_tick, int32_t quirks, float force_rand,
+                     const splat_material_t& material, const SplatParams& sp) {
+    BatchItem it;
+    std::memset(&it, 0, sizeof(it));
+    it.ftri = sc.ftri;
+    it.brute = sc.brute;
+    it.nodes4 = sc.nodes4;
+    it.bvh_tris = sc.bvh_tris;
+    it.n_recs = sc.n_recs;
+    it.n_tris = sc.n_tris;
+    it.first_diffuse = sc.first_diffuse;
+    it.hitter = hitter;
+    it.depth = depth;
+    it.start_tick = start_tick;
+    it.quirks = quirks;
+    it.force_rand = force_rand;
+    it.gen = gen;
+    it.n_rays = n_rays;
+    it.material = material;
+    it.sp = sp;
+    std::memcpy(dst, &it, sizeof(it));
+}
+
+void batch_clear_item(void* dst) {
+    BatchItem it;
+    std::memset(&it, 0, sizeof(it));
+    it.start_tick = -1;
+    std::memcpy(dst, &it, sizeof(it));
+}
+
+void batch_set_seed(void* dst, uint64_t seed) { reinterpret_cast<BatchItem*>(dst)->gen.seed = seed; }
+
+}  // namespace splat

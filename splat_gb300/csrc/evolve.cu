@@ -155,25 +155,13 @@ __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
         if (k < n) {
             r = load_ray(A.in, k);
             id = A.in.id[k];
-            int32_t i = A.hit_idx[k];
-            if (i < 1 || i > A.n_tris) {
-                atomicOr(A.err, 16);
-                i = 1;
-            }
-            const Tri T = load_tri(A.tris, i);
-            HitDerivs h;
-            ih = get_hit_ad(r, i, T, h);
-            if (ih >= A.first_diffuse) {
-                dif = true;
-                if (TRACE) final_evolution(r, h, ih, o);
-                else ray_to_aos(A.aos[id], r, kStatusDiffuse);
-            } else if (isinf(h.t)) {
-                if (!TRACE) ray_to_aos(A.aos[id], r, kStatusInfinity);
-            } else if (!TRACE || !A.last) {
-                const float u = A.force_rand >= 0.0f ? A.force_rand : fresnel_draw(A.seed, id, A.bounce);
-                handle_optics(r, h, ih, T, A.material, u, quirks, o);
-                keep = true;
-            }
+            const EvolveView v{A.tris, A.n_tris, A.err, A.first_diffuse, A.material, A.seed, A.bounce,
+                               A.force_rand, quirks, A.last != 0};
+            const int fate = evolve_one<TRACE>(r, A.hit_idx[k], id, v, o, ih);
+            keep = fate == kFateKeep;
+            dif = fate == kFateDiffuse;
+            if (!TRACE && fate == kFateDiffuse) ray_to_aos(A.aos[id], r, kStatusDiffuse);
+            if (!TRACE && fate == kFateInfinity) ray_to_aos(A.aos[id], r, kStatusInfinity);
         }
         // compaction of the survivors (and, tracing, of the diffuse rays into
         // the splat queue): ballot -> block scan -> one atomic per block each
@@ -210,7 +198,7 @@ __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
 
 static int evolve_grid(int64_t cap, int sm_count) {
     int64_t b = (cap + kEvolveThreads - 1) / kEvolveThreads;
-    const int64_t lim = (int64_t)sm_count * 8;
+    const int64_t lim = (int64_t)sm_count * g_tune[SPLAT_TUNE_EVOLVE_BLOCKS_PER_SM];
     if (b > lim) b = lim;
     return (int)(b < 1 ? 1 : b);
 }
@@ -274,14 +262,6 @@ cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_
 // runs of samples that land on the same texel in a register before one
 // atomic.  Integer maps are therefore bit-exact; float maps change only the
 // summation order, which float atomics never fix anyway.
-__device__ __forceinline__ void flush_texel(const SplatParams& sp, int32_t off, int32_t vi, float vf) {
-    if (off < 0) return;
-    if (sp.accum == SPLAT_ACCUM_I32)
-        atomicAdd(reinterpret_cast<int*>(sp.map) + off, vi);
-    else
-        atomicAdd(reinterpret_cast<float*>(sp.map) + off, vf);
-}
-
 __global__ void __launch_bounds__(256, 3) splat_kernel(RaySoA q, const int64_t* __restrict__ d_count,
                                                     const splat_ftri_t* __restrict__ tris, SplatParams sp,
                                                     splat_trace_stats_t* st) {
@@ -292,9 +272,6 @@ __global__ void __launch_bounds__(256, 3) splat_kernel(RaySoA q, const int64_t* 
     const int sub = lane >> sp.lanes_log2;
     const int sl = lane & (lpr - 1);
     const int planes = sp.n_lambda > 0 ? sp.n_lambda : 1;
-    const int nd = sp.n_delta;
-    const int32_t W = (int32_t)sp.w, H = (int32_t)sp.h;
-    const float Wf = (float)W, Hf = (float)H;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     int done = 0;
@@ -304,46 +281,7 @@ __global__ void __launch_bounds__(256, 3) splat_kernel(RaySoA q, const int64_t* 
         const RayState r = load_ray(q, k);
         const Tri T = load_tri(tris, r.ignore);
         const TriUV quv = tri_uv(T);
-        for (int il = sl; il < planes; il += lpr) {
-            const float lam = sp.n_lambda > 0 ? sp.spectrum[il] : r.lam;
-            const float dl = lam - r.lam;
-            const F3 pe = r.pos + r.dpl * dl;
-            const F3 de = r.dir + r.ddl * dl;
-            const int32_t plane_off = il * W * H;
-            int32_t run_off = -1, run_i = 0;
-            float run_f = 0.f;
-            for (int iy = 0; iy < nd; ++iy) {
-                const float dy = (r.y + sp.deltas[iy]) - r.y;
-                for (int ix = 0; ix < nd; ++ix) {
-                    const float dx = (r.x + sp.deltas[ix]) - r.x;
-                    const F3 pos = (pe + r.dpx * dx) + r.dpy * dy;
-                    const F3 dir = (de + r.ddx * dx) + r.ddy * dy;
-                    const float bu = dot(quv.N, cross(quv.e1, pos - T.b)) / quv.denom;
-                    const float bv = dot(quv.N, cross(quv.e2, pos - T.c)) / quv.denom;
-                    const float bw = (1.0f - bu) - bv;
-                    const float U = (T.ta.x * bu + T.tb.x * bv) + T.tc.x * bw;
-                    const float V = (T.ta.y * bu + T.tb.y * bv) + T.tc.y * bw;
-                    if (isnan(U) || isnan(V) || isinf(U) || isinf(V)) continue;
-                    const float ci = fminf(fmaxf(ceilf(U * Wf), 1.0f), Wf);
-                    const float cj = fminf(fmaxf(ceilf(V * Hf), 1.0f), Hf);
-                    const int32_t off = plane_off + ((int32_t)ci - 1) + ((int32_t)cj - 1) * W;
-                    const F3 nn = (T.na * bu + T.nb * bv) + T.nc * bw;
-                    const float inten = fabsf(dot(normalize(nn), normalize(dir)));
-                    ++done;
-                    const int32_t vi = __float2int_rn(inten * sp.scale);
-                    if (off == run_off) {
-                        run_i += vi;
-                        run_f += inten;
-                    } else {
-                        flush_texel(sp, run_off, run_i, run_f);
-                        run_off = off;
-                        run_i = vi;
-                        run_f = inten;
-                    }
-                }
-            }
-            flush_texel(sp, run_off, run_i, run_f);
-        }
+        for (int il = sl; il < planes; il += lpr) done += splat_ray_plane(sp, r, T, quv, il);
     }
     add_stats(st, 0, done);
 }
@@ -353,7 +291,7 @@ cudaError_t launch_splat(const RaySoA& q, const int64_t* d_count, const splat_ft
     if (q.cap <= 0) return cudaSuccess;
     const int rpw = 32 >> sp.lanes_log2;
     int64_t b = (q.cap + (int64_t)rpw * 8 - 1) / ((int64_t)rpw * 8);
-    const int64_t lim = (int64_t)sm_count * 8;
+    const int64_t lim = (int64_t)sm_count * g_tune[SPLAT_TUNE_SPLAT_BLOCKS_PER_SM];
     if (b > lim) b = lim;
     splat_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_count, tris, sp, stats);
     ++g_launches;
@@ -374,47 +312,6 @@ cudaError_t launch_stats_finish(const int64_t* counts, int depth, const int64_t*
     stats_finish_kernel<<<1, 32, 0, s>>>(counts, depth, splat_count, stats, err);
     ++g_launches;
     return cudaGetLastError();
-}
-
-// ---------------------------------------------------------------------------
-// ray generation, src/ray_generators.jl:64-97
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float gen_lambda(const splat_lambda_mode_t& lm, uint32_t k, float u) {
-    if (lm.mode == SPLAT_LAMBDA_UNIFORM) return lm.lambda0 + (lm.lambda1 - lm.lambda0) * u;
-    if (lm.mode == SPLAT_LAMBDA_STRATIFIED) {
-        const float width = (lm.lambda1 - lm.lambda0) / (float)lm.n_strata;
-        return lm.lambda0 + ((float)(k % (uint32_t)lm.n_strata) + u) * width;
-    }
-    return lm.lambda0;
-}
-
-__device__ __forceinline__ RayState gen_ray(const GenParams& g, int64_t kid) {
-    const int64_t h = g.light.res1 / g.upscale, w = g.light.res2 / g.upscale;
-    const int64_t row = kid % h + 1, col = kid / h + 1;
-    const uint4 rnd = philox(make_uint4((uint32_t)kid, g.light_index, 0u, 0u), (uint32_t)g.seed,
-                             (uint32_t)(g.seed >> 32));
-    const float ddx = uniform24(rnd.x), ddy = uniform24(rnd.y);
-    const float xf = (float)row + ddx, yf = (float)col + ddy;
-    const float h2 = (float)(h / 2), w2 = (float)(w / 2);
-    const F3 C = f3(g.light.center), d1 = f3(g.light.dim1), d2 = f3(g.light.dim2);
-    const float sx = xf - h2, sy = yf - w2;
-    const F3 A = {(d1.x * sx) / h2, (d1.y * sx) / h2, (d1.z * sx) / h2};
-    const F3 B = {(d2.x * sy) / w2, (d2.y * sy) / w2, (d2.z * sy) / w2};
-    RayState r;
-    r.pos = (C + A) + B;
-    r.dpl = {0.f, 0.f, 0.f};
-    r.dpx = {d1.x / h2, d1.y / h2, d1.z / h2};
-    r.dpy = {d2.x / w2, d2.y / w2, d2.z / w2};
-    r.dir = f3(g.light.dir);
-    r.ddl = {0.f, 0.f, 0.f};
-    r.ddx = {0.f, 0.f, 0.f};
-    r.ddy = {0.f, 0.f, 0.f};
-    r.lam = gen_lambda(g.lm, (uint32_t)kid, uniform24(rnd.z));
-    r.x = xf;
-    r.y = yf;
-    r.ignore = 1;
-    r.medium = 0;
-    return r;
 }
 
 __global__ void generate_soa_kernel(GenParams g, int64_t n, RaySoA out, int64_t* d_count) {

@@ -1,0 +1,226 @@
+// hitcore.cuh -- per-ray pieces of the hitters, shared by the single-scene
+// kernels (hit.cu) and the multi-scene batch kernels (batch.cu).
+#pragma once
+
+#include "kernels.h"
+
+namespace splat {
+
+// ---------------------------------------------------------------------------
+// ray loading
+// ---------------------------------------------------------------------------
+struct HitRay {
+    float ox, oy, oz, dx, dy, dz;
+    int32_t ig;
+};
+
+template <bool AOS>
+__device__ __forceinline__ HitRay load_hit_ray(const RaySrc& s, int64_t k) {
+    HitRay r;
+    if (AOS) {
+        const splat_adray_t& a = s.aos[k];
+        r.ox = a.pos[0];
+        r.oy = a.pos[1];
+        r.oz = a.pos[2];
+        r.dx = a.dir[0];
+        r.dy = a.dir[1];
+        r.dz = a.dir[2];
+        r.ig = (int32_t)a.ignore_tri;
+    } else {
+        const float* f = s.f;
+        const int64_t c = s.cap;
+        r.ox = f[k];
+        r.oy = f[c + k];
+        r.oz = f[2 * c + k];
+        r.dx = f[3 * c + k];
+        r.dy = f[4 * c + k];
+        r.dz = f[5 * c + k];
+        r.ig = s.ignore[k];
+    }
+    return r;
+}
+
+// Plane terms of distance_to_plane (src/geo.jl:433-435) and a conservative
+// pre-test: an accepted hit has t = num / den > 0 (so num, den are non-zero
+// with one sign) and t <= best; |num| > |den| best (1 + 2^-20), evaluated in
+// binary32, implies fl(num / den) > best whatever the roundings.  Triangles
+// failing the pre-test could never be accepted, so skipping them leaves the
+// result bit-identical.
+__device__ __forceinline__ bool tri_candidate(const float4& q0, const HitRay& r, float best, float& num, float& den) {
+    num = q0.w - ((q0.x * r.ox + q0.y * r.oy) + q0.z * r.oz);
+    den = (q0.x * r.dx + q0.y * r.dy) + q0.z * r.dz;
+    const bool same_sign = ((num > 0.0f) & (den > 0.0f)) | ((num < 0.0f) & (den < 0.0f));
+    return same_sign & !(fabsf(num) > (fabsf(den) * best) * (1.0f + 0x1p-20f));
+}
+
+// The rest of the reference's test on one hoisted record (src/geo.jl:433-466).
+__device__ __forceinline__ float tri_t_from(float num, float den, const float4& q1, const float4& q2,
+                                            const float4& q3, const float4& q4, const HitRay& r, bool& inside) {
+    float t = num / den;
+    float px = r.ox + r.dx * t;
+    float py = r.oy + r.dy * t;
+    float pz = r.oz + r.dz * t;
+    float v2x = px - q1.x, v2y = py - q1.y, v2z = pz - q1.z;
+    float d02 = (q2.x * v2x + q2.y * v2y) + q2.z * v2z;
+    float d12 = (q3.x * v2x + q3.y * v2y) + q3.z * v2z;
+    float u = (q3.w * d02 - q4.x * d12) * q4.y;
+    float v = (q2.w * d12 - q4.x * d02) * q4.y;
+    inside = (u >= 0.0f) & (v >= 0.0f) & (u + v < 1.0f);
+    return t;
+}
+
+// The reference's test on one hoisted record (src/geo.jl:433-466).
+__device__ __forceinline__ float tri_t(const float4& q0, const float4& q1, const float4& q2, const float4& q3,
+                                       const float4& q4, const HitRay& r, bool& inside) {
+    float num = q0.w - ((q0.x * r.ox + q0.y * r.oy) + q0.z * r.oz);
+    float den = (q0.x * r.dx + q0.y * r.dy) + q0.z * r.dz;
+    float t = num / den;
+    float px = r.ox + r.dx * t;
+    float py = r.oy + r.dy * t;
+    float pz = r.oz + r.dz * t;
+    float v2x = px - q1.x, v2y = py - q1.y, v2z = pz - q1.z;
+    float d02 = (q2.x * v2x + q2.y * v2y) + q2.z * v2z;
+    float d12 = (q3.x * v2x + q3.y * v2y) + q3.z * v2z;
+    float u = (q3.w * d02 - q4.x * d12) * q4.y;
+    float v = (q2.w * d12 - q4.x * d02) * q4.y;
+    inside = (u >= 0.0f) & (v >= 0.0f) & (u + v < 1.0f);
+    return t;
+}
+
+__device__ __forceinline__ float safe_inv(float d) {
+    return 1.0f / (fabsf(d) > 1.0e-30f ? d : copysignf(1.0e-30f, d));
+}
+
+__device__ __forceinline__ float comp(const float4& v, int i) {
+    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+#define SPLAT_CSWAP(ka, ra, kb, rb)       \
+    if (kb < ka) {                         \
+        const float tk = ka;               \
+        ka = kb;                           \
+        kb = tk;                           \
+        const int tr = ra;                 \
+        ra = rb;                           \
+        rb = tr;                           \
+    }
+
+// Closest hit of one ray in a four-wide BVH.  A node fetch (128 bytes)
+// tests four child boxes; hit children are sorted by entry distance, the
+// nearest is visited next and the others are pushed farthest first with
+// their entry distance, so a popped entry beyond the current best hit is
+// skipped.  stack_ref / stack_t hold kBvhStack entries.
+__device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bvh, int* stack_ref, float* stack_t,
+                                             int32_t* err, float& best_out, int32_t& bi_out) {
+    const float kInf = __int_as_float(0x7f800000);
+    const float kMax = 3.402823466e38f;
+    const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
+    const float oix = r.ox * ix, oiy = r.oy * iy, oiz = r.oz * iz;
+    float best = kInf;
+    int32_t bi = 1;
+    int sp = 0;
+    int ref = 0;
+    while (true) {
+        if (ref >= 0) {
+            const Bvh4Node* nd = bvh.nodes + ref;
+            const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix);
+            const float4 ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
+            const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+            const int4 c = __ldg(&nd->c);
+            const int nc = __ldg(&nd->meta.x);
+            float key[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float a0 = fmaf(comp(lx, i), ix, -oix), b0 = fmaf(comp(hx, i), ix, -oix);
+                const float a1 = fmaf(comp(ly, i), iy, -oiy), b1 = fmaf(comp(hy, i), iy, -oiy);
+                const float a2 = fmaf(comp(lz, i), iz, -oiz), b2 = fmaf(comp(hz, i), iz, -oiz);
+                const float tmin = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fminf(a2, b2));
+                const float tmax = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fmaxf(a2, b2));
+                const bool h = (i < nc) & (tmin <= tmax) & (tmax >= 0.0f) & (tmin <= best);
+                key[i] = h ? fminf(tmin, kMax) : kInf;
+            }
+            float k0 = key[0], k1 = key[1], k2 = key[2], k3 = key[3];
+            int r0 = c.x, r1 = c.y, r2 = c.z, r3 = c.w;
+            SPLAT_CSWAP(k0, r0, k1, r1);
+            SPLAT_CSWAP(k2, r2, k3, r3);
+            SPLAT_CSWAP(k0, r0, k2, r2);
+            SPLAT_CSWAP(k1, r1, k3, r3);
+            SPLAT_CSWAP(k1, r1, k2, r2);
+            if (k0 < kInf) {
+                if (sp + 3 <= kBvhStack) {
+                    if (k3 < kInf) {
+                        stack_ref[sp] = r3;
+                        stack_t[sp++] = k3;
+                    }
+                    if (k2 < kInf) {
+                        stack_ref[sp] = r2;
+                        stack_t[sp++] = k2;
+                    }
+                    if (k1 < kInf) {
+                        stack_ref[sp] = r1;
+                        stack_t[sp++] = k1;
+                    }
+                } else {
+                    atomicOr(err, 2);
+                }
+                ref = r0;
+                continue;
+            }
+        } else {
+            const int enc = ~ref;
+            const int first = enc >> 4;
+            const int count = (enc & 15) + 1;
+            for (int j = 0; j < count; ++j) {
+                const TriHit* h = bvh.tris + first + j;
+                float num, den;
+                if (!tri_candidate(__ldg(&h->n_nv), r, best, num, den)) continue;
+                const float4 q1 = __ldg(&h->a_idx);
+                const int32_t idx = __float_as_int(q1.w);
+                bool inside;
+                const float t = tri_t_from(num, den, q1, __ldg(&h->e0), __ldg(&h->e1), __ldg(&h->inv), r, inside);
+                if (inside & (t > 0.0f) & (idx != r.ig) & ((t < best) | ((t == best) & (idx < bi)))) {
+                    best = t;
+                    bi = idx;
+                }
+            }
+        }
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (stack_t[sp] <= best) {
+                ref = stack_ref[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    best_out = best;
+    bi_out = bi;
+}
+#undef SPLAT_CSWAP
+
+// Closest hit of one ray over hit records in reference-index order (the
+// per-ray form of the brute-force hitter; strict < keeps the smaller index).
+__device__ __forceinline__ void brute_closest(const HitRay& r, const TriHit* recs, int64_t n_recs, float& best_out,
+                                              int32_t& bi_out) {
+    float best = __int_as_float(0x7f800000);
+    int32_t bi = 1;
+    for (int64_t j = 0; j < n_recs; ++j) {
+        const TriHit* h = recs + j;
+        float num, den;
+        if (!tri_candidate(__ldg(&h->n_nv), r, best, num, den)) continue;
+        const float4 q1 = __ldg(&h->a_idx);
+        const int32_t idx = __float_as_int(q1.w);
+        bool inside;
+        const float t = tri_t_from(num, den, q1, __ldg(&h->e0), __ldg(&h->e1), __ldg(&h->inv), r, inside);
+        if (inside & (t > 0.0f) & (idx != r.ig) & (t < best)) {
+            best = t;
+            bi = idx;
+        }
+    }
+    best_out = best;
+    bi_out = bi;
+}
+
+}  // namespace splat

@@ -10,6 +10,8 @@ namespace splat {
 
 // Kernels launched by this thread (for launch profiling).
 extern thread_local int64_t g_launches;
+// Launch-shape knobs, indexed by SPLAT_TUNE_* (blocks per SM).
+extern int32_t g_tune[SPLAT_TUNE_KEYS];
 
 // Where a hit kernel reads its rays: the structure-of-arrays bounce state
 // (count on the device) or the reference's AoS ADRay array.
@@ -139,5 +141,41 @@ cudaError_t launch_stats_finish(const int64_t* counts, int depth, const int64_t*
                                 splat_trace_stats_t* stats, const int32_t* err, cudaStream_t s);
 cudaError_t launch_unpack_hits(const uint64_t* tmp, int64_t n, const int64_t* d_count, int32_t* hit_idx,
                                float* hit_t, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// batch engine (batch.cu)
+// ---------------------------------------------------------------------------
+struct BatchSceneRef {
+    const splat_ftri_t* ftri;
+    const TriHit* brute;
+    const Bvh4Node* nodes4;
+    const TriHit* bvh_tris;
+    int64_t n_recs, n_tris, first_diffuse;
+};
+
+struct BatchTickArgs {
+    void* items;  // device item table
+    int n_slots;
+    int tick;
+    void* fresh;  // device FreshList
+    RaySoA cur, next, queue;
+    int64_t* cur_count;
+    int64_t* next_count;
+    int64_t* queue_count;
+    int64_t fresh_rays;  // rays generated this tick (known on the host)
+    int64_t cap_rays;    // bound on the rays active this tick
+    int32_t* hit_idx;
+    int32_t* err;
+    int sm_count;
+};
+
+cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s);
+size_t batch_item_bytes();
+size_t batch_fresh_bytes();
+void batch_fill_item(void* dst, const BatchSceneRef& sc, const GenParams& gen, int64_t n_rays, int32_t depth,
+                     int32_t hitter, int32_t start_tick, int32_t quirks, float force_rand,
+                     const splat_material_t& material, const SplatParams& sp);
+void batch_clear_item(void* dst);
+void batch_set_seed(void* dst, uint64_t seed);
 
 }  // namespace splat

@@ -14,7 +14,7 @@
 // partials -- and through them the fixed-point light map -- reproducible.
 #pragma once
 
-#include "common.cuh"
+#include "kernels.h"
 
 namespace splat {
 
@@ -250,6 +250,51 @@ __device__ __forceinline__ void handle_optics(const RayState& r, const HitDerivs
     o.ignore = i;
 }
 
+// Per-ray parameters of one evolve (one scene, one bounce).
+struct EvolveView {
+    const splat_ftri_t* tris;
+    int64_t n_tris;
+    int32_t* err;
+    int64_t first_diffuse;
+    splat_material_t material;
+    uint64_t seed;
+    uint32_t bounce;
+    float force_rand;
+    bool quirks;
+    bool last;  // trace mode: the last bounce, survivors are dropped
+};
+
+constexpr int kFateDrop = 0;      // miss in trace mode, or a survivor of the last bounce
+constexpr int kFateKeep = 1;      // evolved, active in the next bounce (o)
+constexpr int kFateDiffuse = 2;   // hit a diffuse triangle (trace mode: o is final-evolved)
+constexpr int kFateInfinity = 3;  // plugin mode: missed everything
+
+__device__ __forceinline__ void final_evolution(const RayState& r, const HitDerivs& h, int32_t i, RayState& o);
+
+// evolve_ray (src/tracer.jl:181-201) of one active ray whose hit index is
+// i; rng_id keys its Fresnel draw.  Hit indices outside 1..n_tris are
+// reported in the error word and treated as misses.
+template <bool TRACE>
+__device__ __forceinline__ int evolve_one(const RayState& r, int32_t i, uint32_t rng_id, const EvolveView& v,
+                                          RayState& o, int32_t& ih) {
+    if (i < 1 || i > v.n_tris) {
+        atomicOr(v.err, 16);
+        i = 1;
+    }
+    const Tri T = load_tri(v.tris, i);
+    HitDerivs h;
+    ih = get_hit_ad(r, i, T, h);
+    if (ih >= v.first_diffuse) {
+        if (TRACE) final_evolution(r, h, ih, o);
+        return kFateDiffuse;
+    }
+    if (isinf(h.t)) return TRACE ? kFateDrop : kFateInfinity;
+    if (TRACE && v.last) return kFateDrop;
+    const float u = v.force_rand >= 0.0f ? v.force_rand : fresnel_draw(v.seed, rng_id, v.bounce);
+    handle_optics(r, h, ih, T, v.material, u, v.quirks, o);
+    return kFateKeep;
+}
+
 // final_evolution(r, i, t, ...), src/ray_imagers.jl:4-22: position moved onto
 // the hit with its partials; direction and its partials kept.
 __device__ __forceinline__ void final_evolution(const RayState& r, const HitDerivs& h, int32_t i, RayState& o) {
@@ -316,6 +361,108 @@ __device__ __forceinline__ bool splat_sample(const RayState& r, const Tri& T, fl
     F3 n = (T.na * bu + T.nb * bv) + T.nc * bw;
     intensity = fabsf(dot(normalize(n), normalize(dir)));
     return true;
+}
+
+// ---------------------------------------------------------------------------
+// ray generation, src/ray_generators.jl:64-97
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float gen_lambda(const splat_lambda_mode_t& lm, uint32_t k, float u) {
+    if (lm.mode == SPLAT_LAMBDA_UNIFORM) return lm.lambda0 + (lm.lambda1 - lm.lambda0) * u;
+    if (lm.mode == SPLAT_LAMBDA_STRATIFIED) {
+        const float width = (lm.lambda1 - lm.lambda0) / (float)lm.n_strata;
+        return lm.lambda0 + ((float)(k % (uint32_t)lm.n_strata) + u) * width;
+    }
+    return lm.lambda0;
+}
+
+__device__ __forceinline__ RayState gen_ray(const GenParams& g, int64_t kid) {
+    const int64_t h = g.light.res1 / g.upscale, w = g.light.res2 / g.upscale;
+    const int64_t row = kid % h + 1, col = kid / h + 1;
+    const uint4 rnd = philox(make_uint4((uint32_t)kid, g.light_index, 0u, 0u), (uint32_t)g.seed,
+                             (uint32_t)(g.seed >> 32));
+    const float ddx = uniform24(rnd.x), ddy = uniform24(rnd.y);
+    const float xf = (float)row + ddx, yf = (float)col + ddy;
+    const float h2 = (float)(h / 2), w2 = (float)(w / 2);
+    const F3 C = f3(g.light.center), d1 = f3(g.light.dim1), d2 = f3(g.light.dim2);
+    const float sx = xf - h2, sy = yf - w2;
+    const F3 A = {(d1.x * sx) / h2, (d1.y * sx) / h2, (d1.z * sx) / h2};
+    const F3 B = {(d2.x * sy) / w2, (d2.y * sy) / w2, (d2.z * sy) / w2};
+    RayState r;
+    r.pos = (C + A) + B;
+    r.dpl = {0.f, 0.f, 0.f};
+    r.dpx = {d1.x / h2, d1.y / h2, d1.z / h2};
+    r.dpy = {d2.x / w2, d2.y / w2, d2.z / w2};
+    r.dir = f3(g.light.dir);
+    r.ddl = {0.f, 0.f, 0.f};
+    r.ddx = {0.f, 0.f, 0.f};
+    r.ddy = {0.f, 0.f, 0.f};
+    r.lam = gen_lambda(g.lm, (uint32_t)kid, uniform24(rnd.z));
+    r.x = xf;
+    r.y = yf;
+    r.ignore = 1;
+    r.medium = 0;
+    return r;
+}
+
+
+// ---------------------------------------------------------------------------
+// light-map splat of one (ray, plane)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void flush_texel(const SplatParams& sp, int32_t off, int32_t vi, float vf) {
+    if (off < 0) return;
+    if (sp.accum == SPLAT_ACCUM_I32)
+        atomicAdd(reinterpret_cast<int*>(sp.map) + off, vi);
+    else
+        atomicAdd(reinterpret_cast<float*>(sp.map) + off, vf);
+}
+
+// The N x N sub-samples of one (ray, plane), x offset fastest; returns the
+// number of samples accumulated.
+__device__ __forceinline__ int splat_ray_plane(const SplatParams& sp, const RayState& r, const Tri& T,
+                                               const TriUV& quv, int il) {
+    const int nd = sp.n_delta;
+    const int32_t W = (int32_t)sp.w, H = (int32_t)sp.h;
+    const float Wf = (float)W, Hf = (float)H;
+    int done = 0;
+    const float lam = sp.n_lambda > 0 ? sp.spectrum[il] : r.lam;
+    const float dl = lam - r.lam;
+    const F3 pe = r.pos + r.dpl * dl;
+    const F3 de = r.dir + r.ddl * dl;
+    const int32_t plane_off = il * W * H;
+    int32_t run_off = -1, run_i = 0;
+    float run_f = 0.f;
+    for (int iy = 0; iy < nd; ++iy) {
+        const float dy = (r.y + sp.deltas[iy]) - r.y;
+        for (int ix = 0; ix < nd; ++ix) {
+            const float dx = (r.x + sp.deltas[ix]) - r.x;
+            const F3 pos = (pe + r.dpx * dx) + r.dpy * dy;
+            const F3 dir = (de + r.ddx * dx) + r.ddy * dy;
+            const float bu = dot(quv.N, cross(quv.e1, pos - T.b)) / quv.denom;
+            const float bv = dot(quv.N, cross(quv.e2, pos - T.c)) / quv.denom;
+            const float bw = (1.0f - bu) - bv;
+            const float U = (T.ta.x * bu + T.tb.x * bv) + T.tc.x * bw;
+            const float V = (T.ta.y * bu + T.tb.y * bv) + T.tc.y * bw;
+            if (isnan(U) || isnan(V) || isinf(U) || isinf(V)) continue;
+            const float ci = fminf(fmaxf(ceilf(U * Wf), 1.0f), Wf);
+            const float cj = fminf(fmaxf(ceilf(V * Hf), 1.0f), Hf);
+            const int32_t off = plane_off + ((int32_t)ci - 1) + ((int32_t)cj - 1) * W;
+            const F3 nn = (T.na * bu + T.nb * bv) + T.nc * bw;
+            const float inten = fabsf(dot(normalize(nn), normalize(dir)));
+            ++done;
+            const int32_t vi = __float2int_rn(inten * sp.scale);
+            if (off == run_off) {
+                run_i += vi;
+                run_f += inten;
+            } else {
+                flush_texel(sp, run_off, run_i, run_f);
+                run_off = off;
+                run_i = vi;
+                run_f = inten;
+            }
+        }
+    }
+    flush_texel(sp, run_off, run_i, run_f);
+    return done;
 }
 
 }  // namespace splat

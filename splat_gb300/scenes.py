@@ -326,3 +326,82 @@ def scaled_light(light: np.ndarray, res: int) -> np.ndarray:
     out["res1"] = res
     out["res2"] = res
     return out
+
+
+# --------------------------------------------------------------------------
+# batched and served workloads
+# --------------------------------------------------------------------------
+
+
+def _loguniform(rng, lo, hi):
+    return float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+
+
+def mixed_glass(n_tris: int, seed: int):
+    """A glass mesh of exactly n_tris triangles: the smallest displaced
+    icosphere or Menger sponge level with at least n_tris triangles, cut to
+    n_tris (a seeded choice between the two; Menger only up to level 3).
+    Returns (glass tris, 'sphere' | 'menger')."""
+    rng = np.random.default_rng(seed)
+    if rng.uniform() < 0.5 and n_tris <= 96000:
+        level = next(l for l in (1, 2, 3) if 12 * 20 ** l >= n_tris)
+        return menger_tris(level, 2.0, rotation_seed=seed)[:n_tris], "menger"
+    k = next(k for k in range(1, 9) if 20 * 4 ** k >= n_tris)
+    return sphere_tris(k, noise_amp=0.05, noise_seed=seed)[:n_tris], "sphere"
+
+
+def batched_frames(n: int = 64, seed: int = 5) -> list:
+    """Independent frames of uneven size: triangles log-uniform in
+    [500, 200000], rays log-uniform in [2^14, 2^22], depth 2..6, 1..16
+    wavelength planes, map side log-uniform in [256, 2048], int32 maps."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        n_t = int(round(_loguniform(rng, 500, 200000)))
+        rays = _loguniform(rng, 2 ** 14, 2 ** 22)
+        res = max(128, int(round(np.sqrt(rays))))
+        depth = int(rng.integers(2, 7))
+        planes = int(rng.integers(1, 17))
+        side = int(round(_loguniform(rng, 256, 2048)))
+        glass, kind = mixed_glass(n_t, seed * 1000 + i)
+        if kind == "menger":
+            tris, fd = assemble(glass, box_tris(3.0))
+            light = T.rect_light((0.0, 2.6, 0.0), (0.0, -1.0, 0.0), (1.3, 0.0, 0.0), (0.0, 0.0, 1.3), res, res)
+        else:
+            tris, fd = assemble(glass, floor_tris(-1.5, 4.0))
+            light = hemisphere_light(seed * 1000 + i, res, 1.1)
+        out.append(Workload(
+            name=f"batch{i}-{kind}-{n_t}tris-{res * res}rays-d{depth}-{planes}l-{side}",
+            tris=tris, first_diffuse=fd, light=light, upscale=1,
+            lambda_mode=(T.LAMBDA_STRATIFIED, planes, 400.0, 700.0), spectrum=stratified_spectrum(planes),
+            depth=depth, material=CAUCHY_GLASS, map_w=side, map_h=side, accum="i32", hitter="bvh",
+            seed=seed * 7919 + i))
+    return out
+
+
+def served_scene(sid: int):
+    """Scene sid of the serving pool: a level-3 Menger sponge (96,000
+    triangles) rotated by a seeded quaternion, in the 12-triangle box."""
+    return assemble(menger_tris(3, 2.0, rotation_seed=100 + sid), box_tris(3.0))
+
+
+def served_request(rng, scene, first_diffuse: int, rid: int) -> Workload:
+    """Per-request parameters: light direction perturbed by up to 5 degrees,
+    rays / map / depth / planes drawn like the batched frames."""
+    rays = _loguniform(rng, 2 ** 14, 2 ** 22)
+    res = max(128, int(round(np.sqrt(rays))))
+    depth = int(rng.integers(2, 7))
+    planes = int(rng.integers(1, 17))
+    side = int(round(_loguniform(rng, 256, 2048)))
+    ang = np.radians(5.0) * np.sqrt(rng.uniform())
+    phi = rng.uniform(0, 2 * np.pi)
+    d = np.array([np.sin(ang) * np.cos(phi), -np.cos(ang), np.sin(ang) * np.sin(phi)])
+    e = np.array([1.0, 0.0, 0.0])
+    d1 = _normalize(np.cross(d, np.array([0.0, 0.0, 1.0])))
+    d2 = np.cross(d, d1)
+    light = T.rect_light((0.0, 2.6, 0.0), d, 1.3 * d1, 1.3 * d2, res, res)
+    del e
+    return Workload(name=f"req{rid}", tris=scene, first_diffuse=first_diffuse, light=light, upscale=1,
+                    lambda_mode=(T.LAMBDA_STRATIFIED, planes, 400.0, 700.0), spectrum=stratified_spectrum(planes),
+                    depth=depth, material=CAUCHY_GLASS, map_w=side, map_h=side, accum="i32", hitter="bvh",
+                    seed=1000003 + rid)

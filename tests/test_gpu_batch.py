@@ -1,0 +1,141 @@
+"""Batch engine (splat_batch_*): frames of different scenes, ray counts,
+depths, spectra, map sizes and hitters traced together must each give the
+frame splat_trace_forward gives alone -- bit-exact for int32 maps, within
+1e-5 relative L1 for float maps (float atomics add in another order) --
+whether they start together, join while others are in flight, or run as a
+replayed CUDA graph with new seeds."""
+import numpy as np
+import pytest
+
+from helpers import rel_l1
+from splat_gb300 import scenes as S
+from splat_gb300 import types as T
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+@pytest.fixture(scope="module")
+def frames(torch_cuda):
+    """(scene, workload) pairs of very different shapes."""
+    from splat_gb300 import tracer
+
+    out = []
+    tris, fd = S.assemble(S.sphere_tris(2), S.floor_tris(-1.5, 4.0))
+    small = S.Workload(name="s", tris=tris, first_diffuse=fd, light=S.hemisphere_light(3, 80, 1.05), depth=3,
+                       material=S.CAUCHY_GLASS, map_w=48, map_h=40, accum="i32", spectrum=S.stratified_spectrum(3),
+                       lambda_mode=(T.LAMBDA_UNIFORM, 1, 400.0, 700.0), hitter="brute", seed=11)
+    out.append((tracer.Scene(small.tris, small.first_diffuse, bvh=True), small))
+    out.append((out[0][0], small.with_(hitter="bvh", depth=2, seed=12, quirks=False, map_w=64)))
+    rt = S.realtime(light=S.scaled_light(S.realtime().light, 384))
+    out.append((tracer.Scene(rt.tris, rt.first_diffuse, bvh=True), rt))
+    mg = S.menger(light=S.scaled_light(S.menger().light, 160))
+    out.append((tracer.Scene(mg.tris, mg.first_diffuse, bvh=True), mg))
+    ps = S.plain_small(light=S.scaled_light(S.plain_small().light, 120))
+    out.append((tracer.Scene(ps.tris, ps.first_diffuse, bvh=True), ps))  # float map, own wavelength
+    sell = (T.MATERIAL_SELLMEIER, 0.0, 0.0, (1.03961212, 0.231792344, 1.01046945),
+            (0.00600069867, 0.0200179144, 103.560653))
+    out.append((out[2][0], rt.with_(material=sell, depth=5, seed=99, light=S.scaled_light(rt.light, 200))))
+    return out
+
+
+def _alone(scene, wl, seed=None):
+    from splat_gb300 import tracer
+
+    w = wl if seed is None else wl.with_(seed=seed)
+    return tracer.trace_forward(w, scene=scene).tex.cpu().numpy()
+
+
+def _check(wl, got, ref, what):
+    if wl.accum == "i32":
+        bad = np.count_nonzero(got != ref)
+        assert bad == 0, f"{what}: {bad} texels differ"
+    else:
+        assert rel_l1(got, ref) <= 1e-5, what
+    assert ref.sum() > 0, what
+
+
+def test_batch_equals_single_frames(frames):
+    from splat_gb300 import batch, tracer
+
+    b = batch.Batch(16, 1 << 21)
+    texs = []
+    for sc, wl in frames:
+        tex = tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum)
+        b.admit(sc, wl, tex)
+        texs.append(tex)
+    done = b.run()
+    assert sorted(done) == list(range(len(frames)))
+    for i, ((sc, wl), tex) in enumerate(zip(frames, texs)):
+        _check(wl, tex.cpu().numpy(), _alone(sc, wl), f"frame {i}")
+    for s in done:
+        b.release(s)
+    assert b.status()["in_flight"] == 0
+
+
+def test_frames_joining_while_others_run(frames):
+    """Continuous batching: frames admitted at different ticks overlap on the
+    device and each still equals its alone result."""
+    from splat_gb300 import batch, tracer
+
+    b = batch.Batch(8, 1 << 21)
+    plan = {0: [3, 0], 1: [2], 2: [1, 5], 4: [4]}
+    texs, done = {}, []
+    tick = 0
+    while tick <= 4 or b.status()["in_flight"] > 0:
+        for i in plan.get(tick, []):
+            sc, wl = frames[i]
+            texs[i] = (b.admit(sc, wl, tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum)), i)
+            texs[i] = (texs[i][0], b.items[texs[i][0]][2])
+        assert b.status()["in_flight"] > 0 or tick > 4
+        done += b.tick()
+        tick += 1
+    assert len(done) == 6
+    for i, (slot, tex) in texs.items():
+        sc, wl = frames[i]
+        _check(wl, tex.cpu().numpy(), _alone(sc, wl), f"frame {i} joined late")
+
+
+def test_graph_capture_and_replay_with_new_seeds(frames):
+    from splat_gb300 import batch, tracer
+
+    b = batch.Batch(8, 1 << 21)
+    sel = [0, 2, 3]
+    texs = []
+    for i in sel:
+        sc, wl = frames[i]
+        tex = tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum)
+        b.admit(sc, wl, tex)
+        texs.append(tex)
+    n_ticks = b.capture()
+    assert n_ticks == max(frames[i][1].depth for i in sel)
+    for seeds in ([101, 202, 303], [7, 8, 9]):
+        b.replay(seeds)
+        for s, i in enumerate(sel):
+            sc, wl = frames[i]
+            _check(wl, texs[s].cpu().numpy(), _alone(sc, wl, seeds[s]), f"replay frame {i} seed {seeds[s]}")
+
+
+def test_admission_respects_the_pool(frames):
+    from splat_gb300 import batch, tracer
+
+    sc, wl = frames[2]  # 192^2 = 36,864 rays
+    b = batch.Batch(4, 50000)
+    t1 = tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum)
+    s1 = b.admit(sc, wl, t1)
+    with pytest.raises(batch.PoolFull):
+        b.admit(sc, wl, tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum))
+    assert b.run() == [s1]
+    b.release(s1)
+    t2 = tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum)
+    b.admit(sc, wl.with_(seed=5), t2)
+    b.run()
+    _check(wl, t1.cpu().numpy(), _alone(sc, wl), "first")
+    _check(wl, t2.cpu().numpy(), _alone(sc, wl, 5), "second")
