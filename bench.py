@@ -316,7 +316,8 @@ def run_ours(args):
     bytes_per_launch = alg / n_kind_launches
     avg_launch_s = dom_ms / 1e3 / n_kind_launches
     achieved = bytes_per_launch / avg_launch_s / 1e9
-    kernel_name = {"hit_bvh": "hit_bvh_kernel", "hit_brute": "hit_brute_kernel", "evolve": "evolve_kernel",
+    kernel_name = {"hit_bvh": "hit_bvh_kernel" if wl.hitter == "bvh2" else "hit_bvh4_kernel",
+                   "hit_brute": "hit_brute_kernel", "evolve": "evolve_kernel",
                    "splat": "splat_kernel", "generate": "generate_soa_kernel"}[dom]
     traffic = profile_traffic(kernel_name)
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",

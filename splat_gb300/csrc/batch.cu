@@ -102,6 +102,7 @@ __global__ void batch_generate_kernel(const BatchItem* __restrict__ items, const
     }
 }
 
+template <bool ANY_BRUTE>
 __global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t* __restrict__ count,
                                                         const BatchItem* __restrict__ items, int32_t* hit_idx,
                                                         int32_t* err) {
@@ -117,7 +118,7 @@ __global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t
         const BatchItem& it = items[in.id[k] >> kSlotShift];
         float best;
         int32_t bi;
-        if (it.hitter == SPLAT_HITTER_BVH && it.nodes4)
+        if (!ANY_BRUTE || (it.hitter == SPLAT_HITTER_BVH && it.nodes4))
             bvh4_closest(r, Bvh4View{it.nodes4, it.bvh_tris}, stack_ref, stack_t, err, best, bi);
         else
             brute_closest(r, it.brute, it.n_recs, best, bi);
@@ -216,8 +217,11 @@ cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s) {
         ++g_launches;
     }
     if (a.cap_rays > 0) {
-        batch_hit_kernel<<<grid_cap(a.cap_rays, 128, a.sm_count, 16), 128, 0, s>>>(a.cur, a.cur_count, items,
-                                                                                   a.hit_idx, a.err);
+        const int hg = grid_cap(a.cap_rays, 128, a.sm_count, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
+        if (a.any_brute)
+            batch_hit_kernel<true><<<hg, 128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err);
+        else
+            batch_hit_kernel<false><<<hg, 128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err);
         ++g_launches;
         batch_evolve_kernel<<<grid_cap(a.cap_rays, kBatchThreads, a.sm_count, 8), kBatchThreads, 0, s>>>(
             a.cur, a.next, a.queue, a.cur_count, a.next_count, a.queue_count, items, a.tick, a.hit_idx, a.err);

@@ -254,34 +254,22 @@ cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_
     return cudaGetLastError();
 }
 
-// Queued diffuse rays -> light map.  One lane per (ray, wavelength plane):
-// 1 << lanes_log2 lanes share a ray (several rays per warp when it has fewer
-// than 32 planes).  A lane walks its plane's N x N sub-samples in the
-// reference's order (x offset fastest), reusing the first terms of the
-// expansions' left fold (pos + dp/dlambda dlambda, identical bits), and adds
-// runs of samples that land on the same texel in a register before one
-// atomic.  Integer maps are therefore bit-exact; float maps change only the
-// summation order, which float atomics never fix anyway.
+// Queued diffuse rays -> light map, one lane per ray walking all its planes
+// (each plane's N x N sub-samples in the reference's order, x offset
+// fastest; runs of samples on the same texel add in a register before one
+// atomic).  Integer maps are bit-exact; float maps change only the order of
+// additions, which float atomics never fix anyway.
 __global__ void __launch_bounds__(256, 3) splat_kernel(RaySoA q, const int64_t* __restrict__ d_count,
-                                                    const splat_ftri_t* __restrict__ tris, SplatParams sp,
-                                                    splat_trace_stats_t* st) {
+                                                       const splat_ftri_t* __restrict__ tris, SplatParams sp,
+                                                       splat_trace_stats_t* st) {
     const int64_t n = *d_count;
-    const int lane = lane_id();
-    const int lpr = 1 << sp.lanes_log2;
-    const int rpw = 32 >> sp.lanes_log2;
-    const int sub = lane >> sp.lanes_log2;
-    const int sl = lane & (lpr - 1);
     const int planes = sp.n_lambda > 0 ? sp.n_lambda : 1;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     int done = 0;
-    for (int64_t r0 = warp * rpw; r0 < n; r0 += n_warps * rpw) {
-        const int64_t k = r0 + sub;
-        if (k >= n) continue;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
         const RayState r = load_ray(q, k);
         const Tri T = load_tri(tris, r.ignore);
         const TriUV quv = tri_uv(T);
-        for (int il = sl; il < planes; il += lpr) done += splat_ray_plane(sp, r, T, quv, il);
+        for (int il = 0; il < planes; ++il) done += splat_ray_plane(sp, r, T, quv, il);
     }
     add_stats(st, 0, done);
 }
@@ -289,8 +277,7 @@ __global__ void __launch_bounds__(256, 3) splat_kernel(RaySoA q, const int64_t* 
 cudaError_t launch_splat(const RaySoA& q, const int64_t* d_count, const splat_ftri_t* tris, const SplatParams& sp,
                          splat_trace_stats_t* stats, int sm_count, cudaStream_t s) {
     if (q.cap <= 0) return cudaSuccess;
-    const int rpw = 32 >> sp.lanes_log2;
-    int64_t b = (q.cap + (int64_t)rpw * 8 - 1) / ((int64_t)rpw * 8);
+    int64_t b = (q.cap + 255) / 256;
     const int64_t lim = (int64_t)sm_count * g_tune[SPLAT_TUNE_SPLAT_BLOCKS_PER_SM];
     if (b > lim) b = lim;
     splat_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_count, tris, sp, stats);

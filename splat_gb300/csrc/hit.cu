@@ -544,9 +544,24 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_kernel(RaySrc src, Bvh4V
 }
 
 
+// The traversal kernels use no shared memory: give the whole L1/shared
+// array to L1, where the upper BVH levels and hot hit records live.
+template <class K>
+static void prefer_l1(K kernel) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+}
+
 cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh, int32_t* hit_idx, float* hit_t,
                             int32_t* err, int sm_count, cudaStream_t s) {
     if (cap <= 0) return cudaSuccess;
+    static bool configured = false;
+    if (!configured) {
+        prefer_l1(hit_bvh4_kernel<true>);
+        prefer_l1(hit_bvh4_kernel<false>);
+        prefer_l1(hit_bvh_kernel<true>);
+        prefer_l1(hit_bvh_kernel<false>);
+        configured = true;
+    }
     const int grid = grid_for(cap, kBvhThreads, sm_count, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
     if (rays.aos)
         hit_bvh4_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);

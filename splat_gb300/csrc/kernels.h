@@ -167,6 +167,7 @@ struct BatchTickArgs {
     int32_t* hit_idx;
     int32_t* err;
     int sm_count;
+    bool any_brute;      // some item in flight uses the brute-force hitter (or has no BVH)
 };
 
 cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s);
