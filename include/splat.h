@@ -268,6 +268,106 @@ splat_status_t splat_trace_forward_host(splat_scene_t* scene, const splat_ftri_t
                                         void* d_workspace, size_t workspace_bytes, splat_trace_stats_t* host_stats,
                                         void* stream);
 
+/* ------------------------------------------------------------ camera pass */
+/* The backward half of trace! (src/tracer.jl:345-378): camera rays traced
+ * through the same bounce loop, then shaded from the light map the forward
+ * step wrote and from a skydome (continuum_shade!, ExperimentalImager2).
+ *
+ * Cam (src/geo.jl:50-57), Julia layout: 64 bytes. */
+typedef struct splat_camera {
+    float pos[3];
+    float look_at[3];
+    float dir[3];
+    float up[3];
+    float right[3];
+    float fov_half_sin;
+} splat_camera_t;
+
+/* get_camera (src/geo.jl:183-191): dir = normalize(look_at - pos),
+ * right = normalize(dir x true_up), up = normalize(right x dir),
+ * fov_half_sin = sin(fov / 2) (fov in radians, evaluated in double). */
+splat_status_t splat_camera_look_at(const float pos[3], const float look_at[3], const float true_up[3], double fov,
+                                    splat_camera_t* out);
+
+/* wrap_ray_gen(camera_ray) (src/ray_generators.jl:18-62): height * width
+ * camera rays, column-major over (x = row 1..height, y = col 1..width), at
+ * wavelength lambda; dest = (y - 1) * height + x.  The direction and its x / y
+ * derivatives are evaluated in double and rounded once, as the reference's
+ * integer pixel indices promote them.  The jitter dv in [0, 1)^3 is
+ * Philox(seed) keyed by the ray index (the reference draws CUDA.rand). */
+splat_status_t splat_camera_rays(const splat_camera_t* camera, int64_t height, int64_t width, float lambda,
+                                 uint64_t seed, splat_adray_t* d_rays, void* stream);
+
+/* _spectrum_datastructs (src/rgb_spectrum.jl:135-149): retina response of
+ * each wavelength, out[c * n_lambda + i] for c = red, green, blue: the
+ * reference's piecewise-linear retina curves normalised by their sums over
+ * 400..700 nm, evaluated in double and rounded to float (host only). */
+splat_status_t splat_retina_factors(const float* spectrum, int32_t n_lambda, float* out);
+
+/* Shader: the light map and the skydome as hardware-filtered textures
+ * (CuTexture(CuTextureArray(tex); interpolation = LinearInterpolation()),
+ * src/tracer.jl:343 and src/scenes/sphere.jl:116-126): 3-D float arrays,
+ * linear filtering, clamped addressing, unnormalised coordinates.  Library-
+ * owned device arrays, reused frame after frame. */
+typedef struct splat_shader splat_shader_t;
+/* map: [map_w, map_h, n_planes]; sky: [sky_w, sky_h, 3] (sky_w = 0: no
+ * skydome, escaping rays shade black). */
+splat_status_t splat_shader_create(int64_t map_w, int64_t map_h, int32_t n_planes, int64_t sky_w, int64_t sky_h,
+                                   splat_shader_t** out);
+splat_status_t splat_shader_destroy(splat_shader_t* shader);
+/* Loads a light map (device, column-major [w, h, planes]); int32 maps are
+ * converted to float (value / 2^frac_bits) on the way. */
+splat_status_t splat_shader_set_light_map(splat_shader_t* shader, const void* d_map, int32_t accum, int32_t frac_bits,
+                                          void* stream);
+/* Loads the skydome (device float, [sky_w, sky_h, 3] column-major). */
+splat_status_t splat_shader_set_skydome(splat_shader_t* shader, const float* d_sky, void* stream);
+
+/* continuum_shade!(ExperimentalImager2) (src/ray_imagers.jl:441-503) on the
+ * caller's rays after splat_run_evolution (ray i at index dest - 1, hit
+ * indices realigned): final_evolution of the diffuse rays in place, then
+ * for every ray and upscale^2 sub-sample (shade_tex4_kernel,
+ * src/ray_imagers.jl:383-438): diffuse -> sum over the spectrum of
+ * retina * light map texel at the hit's uv; escaped -> skydome at the
+ * direction's polar angles; otherwise black; each channel clamped to
+ * [0, 1].  d_rgb: height * width RGB float triples, column-major pixels
+ * (the reference's RGBf image); camera ray (x, y) sub-sample (i, j) lands on
+ * pixel (upscale (x-1) + i, upscale (y-1) + j).  retina: [3][n_lambda]. */
+splat_status_t splat_continuum_shade(const splat_scene_t* scene, const splat_shader_t* shader, splat_adray_t* d_rays,
+                                     int64_t n_rays, const int32_t* d_hit_idx, const float* spectrum,
+                                     const float* retina, int32_t n_lambda, int64_t upscale, int64_t height,
+                                     int64_t width, float* d_rgb, void* stream);
+
+/* One camera pass in the fused form (SoA, compacted bounce loop). */
+typedef struct splat_render_params {
+    splat_camera_t camera;
+    int64_t height, width;  /* image in pixels; camera rays (height / upscale) x (width / upscale) */
+    int64_t upscale;        /* backward_upscale */
+    uint64_t seed;          /* Philox key: camera jitter and Fresnel draws */
+    int32_t depth;
+    int32_t hitter;         /* SPLAT_HITTER_* */
+    splat_material_t material;
+    float force_rand;       /* < 0: draw */
+    uint32_t flags;         /* SPLAT_FLAG_* */
+    float lambda;           /* camera rays' wavelength (the reference uses 550) */
+    int32_t n_lambda;       /* shading spectrum = the light map's planes */
+    float spectrum[SPLAT_MAX_LAMBDA];
+    float retina[3][SPLAT_MAX_LAMBDA];
+} splat_render_params_t;
+
+size_t splat_render_workspace_size(int64_t n_camera_rays);
+/* Camera rays -> depth x {hit, evolve} with diffuse rays final-evolved into
+ * a shading queue and escaping rays into a sky queue -> shading straight
+ * into their pixels (the rest stay black).  The image equals
+ * splat_camera_rays + splat_run_evolution + splat_continuum_shade. */
+splat_status_t splat_render_camera(const splat_scene_t* scene, const splat_shader_t* shader,
+                                   const splat_render_params_t* params, float* d_rgb, void* d_workspace,
+                                   size_t workspace_bytes, void* stream);
+
+/* Running average of a frame's iterations (src/tracer.jl:380-384):
+ * iteration k = 1 copies rgb into out; k > 1 sets
+ * out = out * (k - 1) / k + rgb / k.  n: floats. */
+splat_status_t splat_image_accumulate(float* d_out, const float* d_rgb, int64_t n, int32_t iteration, void* stream);
+
 /* ----------------------------------------------------------- batch engine */
 /* Many frames of many scenes traced together (the batched and served
  * forms).  An item is one frame: a resident scene, its trace parameters and
@@ -305,15 +405,18 @@ splat_status_t splat_batch_capture(splat_batch_t* batch, void* stream, int32_t* 
 splat_status_t splat_batch_replay(splat_batch_t* batch, const uint64_t* seeds, int32_t n_seeds, void* stream);
 
 /* ---------------------------------------------------------------- tuning */
-/* Launch-shape knobs (blocks per SM of the grid-stride kernels, process-wide).
- * They change only how work is spread over the GPU, never a result; the
- * autotuner (splat_gb300/autotune.py) picks them per workload. */
+/* Launch-shape knobs (process-wide): blocks per SM of the grid-stride
+ * kernels (1..256), and the splat's block-level texel aggregation (0 or 1).
+ * They change only how work is spread over the GPU, never a result (float
+ * maps: summation order only); the autotuner (splat_gb300/autotune.py)
+ * picks them per workload. */
 enum {
     SPLAT_TUNE_BRUTE_BLOCKS_PER_SM = 0, /* brute force: triangle-range splits target (default 4) */
     SPLAT_TUNE_BVH_BLOCKS_PER_SM = 1,   /* BVH traversal grid (default 16) */
     SPLAT_TUNE_EVOLVE_BLOCKS_PER_SM = 2, /* evolve grid (default 8) */
     SPLAT_TUNE_SPLAT_BLOCKS_PER_SM = 3,  /* splat grid (default 8) */
-    SPLAT_TUNE_KEYS = 4
+    SPLAT_TUNE_SPLAT_AGGREGATE = 4,      /* splat sums samples per texel in shared memory first (default 0) */
+    SPLAT_TUNE_KEYS = 5
 };
 splat_status_t splat_set_tuning(int32_t key, int32_t value);
 int32_t splat_get_tuning(int32_t key);
@@ -331,7 +434,8 @@ enum {
     SPLAT_KERNEL_AUX = 4, /* fills, unpacks, conversions, stats, refit, packing */
     SPLAT_KERNEL_SPLAT = 5,
     SPLAT_KERNEL_BATCH = 6, /* one whole batch tick */
-    SPLAT_KERNEL_KINDS = 7
+    SPLAT_KERNEL_SHADE = 7, /* camera pass: camera rays, light-map / skydome shading, texture uploads */
+    SPLAT_KERNEL_KINDS = 8
 };
 typedef struct splat_profile splat_profile_t;
 splat_status_t splat_profile_create(int32_t max_launches, splat_profile_t** out);

@@ -750,3 +750,184 @@ void o_trace_forward(const o_rect_light* light, int64_t upscale, const o_lambda_
     free(ids);
     if (!rays_out) free(rays);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Camera pass, src/geo.jl:183-191, src/ray_generators.jl:18-62,            */
+/* src/ray_imagers.jl:383-503                                                */
+/* ------------------------------------------------------------------------ */
+void o_camera_look_at(const float pos[3], const float look_at[3], const float true_up[3], double fov, o_camera* out) {
+    memset(out, 0, sizeof(*out));
+    for (int i = 0; i < 3; ++i) {
+        out->pos[i] = pos[i];
+        out->look_at[i] = look_at[i];
+    }
+    v3 dir = vnormalize(vsub(V(look_at), V(pos)));
+    v3 right = vnormalize(vcross(dir, V(true_up)));
+    v3 up = vnormalize(vcross(right, dir));
+    vstore(out->dir, dir);
+    vstore(out->right, right);
+    vstore(out->up, up);
+    out->fov_half_sin = (float)sin(fov / 2.0);
+}
+
+/* One ForwardDiff partial in double. */
+typedef struct { double v, d; } ddual;
+
+void o_camera_rays(const o_camera* cam, int64_t h, int64_t w, float lambda, uint64_t seed, o_adray* out) {
+    const double cos45 = 1.0 / sqrt(2.0);
+    const double scale = ((double)h * cos45) / (double)cam->fov_half_sin;
+    const float m = (float)(h > w ? h : w);
+    for (int64_t g = 0; g < h * w; ++g) {
+        const int64_t x = g % h + 1, y = g / h + 1;
+        uint32_t rnd[4];
+        draw4(seed, (uint32_t)g, 0u, 2u, 0u, rnd);
+        const float dv[3] = {(o_uniform(rnd[0]) * 0.025f) / m, (o_uniform(rnd[1]) * 0.025f) / m,
+                             (o_uniform(rnd[2]) * 0.025f) / m};
+        /* x pass: _x carries the partial; y pass: _y does. */
+        ddual X = {((double)x - (double)h / 2.0) / scale, 1.0 / scale};
+        ddual Y = {((double)y - (double)w / 2.0) / scale, 1.0 / scale};
+        const double x2 = X.v * X.v, y2 = Y.v * Y.v;
+        const double zz = (1.0 - x2) - y2;
+        const double z = sqrt(zz);
+        const double dsq = 1.0 / (2.0 * z);
+        const double zx = (-((X.d * 2.0) * X.v)) * dsq; /* d(1 - _x^2 - _y^2)/dx through sqrt */
+        const double zy = (-((Y.d * 2.0) * Y.v)) * dsq;
+        o_adray* r = &out[g];
+        memset(r, 0, sizeof(*r));
+        for (int i = 0; i < 3; ++i) {
+            const double R = cam->right[i], U = cam->up[i], D = cam->dir[i];
+            r->pos[i] = cam->pos[i];
+            r->dir[i] = (float)((((X.v * R) + (Y.v * U)) + (z * D)) + (double)dv[i]);
+            r->dd_dx[i] = (float)((X.d * R) + (zx * D));
+            r->dd_dy[i] = (float)((Y.d * U) + (zy * D));
+        }
+        r->in_medium = 0;
+        r->ignore_tri = 1;
+        r->dest = (y - 1) * h + x;
+        r->lambda = lambda;
+        r->x = 0.0f;
+        r->y = 0.0f;
+        r->status = O_STATUS_ACTIVE;
+    }
+}
+
+/* CUDA texture fetch at CUDA coordinates (x, y, z) (the reference's
+ * 1-based coordinate minus 0.5), linear filter, clamp addressing,
+ * unnormalised coordinates: xB = x - 0.5, i = floor(xB), a = xB - i, texels
+ * i and i + 1 clamped to the array.  Returns the exactly-weighted value; *spread is the
+ * largest difference between the texels that carry weight. */
+static double tex_fetch(const float* a, int64_t W, int64_t H, int64_t D, float x, float y, float z, double* spread) {
+    if (!isfinite(x) || !isfinite(y) || !isfinite(z)) {
+        *spread = INFINITY;
+        return NAN;
+    }
+    const double c[3] = {(double)x - 0.5, (double)y - 0.5, (double)z - 0.5};
+    const int64_t ext[3] = {W, H, D};
+    int64_t i0[3], i1[3];
+    double f[3];
+    for (int k = 0; k < 3; ++k) {
+        const double fl = floor(c[k]);
+        f[k] = c[k] - fl;
+        int64_t lo = (int64_t)fl, hi = lo + 1;
+        lo = lo < 0 ? 0 : (lo > ext[k] - 1 ? ext[k] - 1 : lo);
+        hi = hi < 0 ? 0 : (hi > ext[k] - 1 ? ext[k] - 1 : hi);
+        i0[k] = lo;
+        i1[k] = hi;
+    }
+    double v = 0.0, mn = INFINITY, mx = -INFINITY;
+    for (int dz = 0; dz < 2; ++dz)
+        for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx) {
+                const double wgt = (dx ? f[0] : 1.0 - f[0]) * (dy ? f[1] : 1.0 - f[1]) * (dz ? f[2] : 1.0 - f[2]);
+                const int live = (dx == 0 || f[0] > 0.0) && (dy == 0 || f[1] > 0.0) && (dz == 0 || f[2] > 0.0);
+                if (!live) continue;
+                const int64_t xi = dx ? i1[0] : i0[0], yi = dy ? i1[1] : i0[1], zi = dz ? i1[2] : i0[2];
+                const double t = a[xi + W * (yi + H * zi)];
+                v += wgt * t;
+                if (t < mn) mn = t;
+                if (t > mx) mx = t;
+            }
+    *spread = mx - mn;
+    return v;
+}
+
+/* Julia clamp(x, 0, 1): NaN passes through. */
+static float clamp01f(float x) { return x > 1.0f ? 1.0f : (x < 0.0f ? 0.0f : x); }
+
+static void put_px(float* rgb, float* tol, int64_t height, int64_t cam_h, int32_t nd, int64_t ray, int i, int j,
+                   const double val[3], const double tl[3]) {
+    const int64_t gx = ray % cam_h, gy = ray / cam_h;
+    const int64_t px = ((int64_t)nd * gx + i) + height * ((int64_t)nd * gy + j);
+    for (int c = 0; c < 3; ++c) {
+        rgb[3 * px + c] = clamp01f((float)val[c]);
+        tol[3 * px + c] = (float)tl[c];
+    }
+}
+
+void o_continuum_shade(o_adray* rays, int64_t n_rays, const int32_t* hit_idx, const o_ftri* tris,
+                       const float* spectrum, const float* retina, int32_t n_lambda, int32_t upscale,
+                       const float* tex, int64_t tw, int64_t th, int64_t planes, const float* sky, int64_t sw,
+                       int64_t sh, int64_t height, int64_t width, float* rgb, float* tol) {
+    float deltas[64];
+    const int32_t nd = upscale < 1 ? 1 : (upscale > 64 ? 64 : upscale);
+    o_upres(nd, deltas);
+    const int64_t cam_h = height / nd;
+    const float kPi = 3.14159265358979323846f;
+    /* quantised filter weights: 2^-8 per filtered axis, two axes */
+    const double q = 0x1p-7;
+    (void)width;
+    for (int64_t k = 0; k < n_rays; ++k) {
+        o_adray* r = &rays[k];
+        const int32_t ih = hit_idx[k];
+        const o_ftri* T = &tris[ih - 1];
+        if (r->status == O_STATUS_DIFFUSE) final_evolution(r, ih, T);
+        for (int i = 0; i < nd; ++i) {
+            const float xs = r->x + deltas[i];
+            for (int j = 0; j < nd; ++j) {
+                const float ys = r->y + deltas[j];
+                double val[3] = {0, 0, 0}, tl[3] = {0, 0, 0};
+                if (r->status == O_STATUS_INFINITY && sky) {
+                    v3 d = dval(d_expansion(r, DC(r->lambda), DC(xs), DC(ys)));
+                    const float th_ = acosf(d.z);
+                    const float ph = atan2f(d.y, d.x);
+                    const float vv = ((ph / kPi) + 1.0f) * 0.5f;
+                    const float uu = th_ / kPi;
+                    const float us = uu * (float)sw, vs = vv * (float)sh;
+                    for (int c = 0; c < 3; ++c) {
+                        double sp;
+                        val[c] = tex_fetch(sky, sw, sh, 3, us - 0.5f, vs - 0.5f, (float)c + 0.5f, &sp);
+                        /* + a few ulp of the polar angles (acosf / atan2f differ between libraries) */
+                        tl[c] = (q + 0x1p-10) * sp + 0x1p-20 * fabs(val[c]);
+                    }
+                } else if (r->status == O_STATUS_DIFFUSE) {
+                    float R = 0.0f, G = 0.0f, B = 0.0f;
+                    for (int32_t il = 0; il < n_lambda; ++il) {
+                        v3 pos = dval(p_expansion(r, DC(spectrum[il]), DC(xs), DC(ys)));
+                        float bu, bv;
+                        reverse_uv_f(pos, T, &bu, &bv);
+                        const float bw = (1.0f - bu) - bv;
+                        const float U = (T->v[7][0] * bu + T->v[8][0] * bv) + T->v[9][0] * bw;
+                        const float Vt = (T->v[7][1] * bu + T->v[8][1] * bv) + T->v[9][1] * bw;
+                        if (isnan(U) || isnan(Vt)) continue;
+                        double sp;
+                        const float X = (float)tex_fetch(tex, tw, th, planes, U * (float)tw - 0.5f,
+                                                         Vt * (float)th - 0.5f, (float)(il + 1) - 0.5f, &sp);
+                        const float rr = retina[il], gg = retina[n_lambda + il], bb = retina[2 * n_lambda + il];
+                        R = R + rr * X;
+                        G = G + gg * X;
+                        B = B + bb * X;
+                        const double e = q * sp + 0x1p-20 * fabs((double)X);
+                        tl[0] += fabs((double)rr) * e;
+                        tl[1] += fabs((double)gg) * e;
+                        tl[2] += fabs((double)bb) * e;
+                    }
+                    val[0] = R;
+                    val[1] = G;
+                    val[2] = B;
+                    for (int c = 0; c < 3; ++c) tl[c] += 0x1p-20 * fabs(val[c]) * (double)(n_lambda + 1);
+                }
+                put_px(rgb, tol, height, cam_h, nd, k, i, j, val, tl);
+            }
+        }
+    }
+}

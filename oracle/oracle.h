@@ -156,6 +156,37 @@ void o_trace_forward(const o_rect_light* light, int64_t upscale, const o_lambda_
                      int32_t frac_bits, int64_t width, int64_t height, int64_t ray_begin,
                      int64_t ray_end, o_adray* rays_out, int64_t* stats, int nthreads);
 
+/* Cam (src/geo.jl:50-57): 64 bytes. */
+typedef struct o_camera {
+    float pos[3];
+    float look_at[3];
+    float dir[3];
+    float up[3];
+    float right[3];
+    float fov_half_sin;
+} o_camera;
+
+/* get_camera (src/geo.jl:183-191). */
+void o_camera_look_at(const float pos[3], const float look_at[3], const float true_up[3], double fov, o_camera* out);
+
+/* wrap_ray_gen(camera_ray) (src/ray_generators.jl:18-62) over an h x w grid:
+ * ray g = (x - 1) + h (y - 1); jitter dv from Philox(seed) at (g, 0, 2, 0).
+ * The direction and its partials are evaluated in double (integer pixel
+ * indices promote them) and rounded to float once. */
+void o_camera_rays(const o_camera* cam, int64_t h, int64_t w, float lambda, uint64_t seed, o_adray* out);
+
+/* continuum_shade!(ExperimentalImager2) (src/ray_imagers.jl:383-503) with a
+ * model of the texture unit's linear filter: exact (unquantised) weights;
+ * tol receives, per image value, a bound on what the hardware's 8-bit
+ * fractional weights and its math library may change (+inf where the
+ * texture coordinate is not finite).  tex: [tw, th, planes] column-major;
+ * sky: [sw, sh, 3] or NULL.  rgb / tol: height * width RGB triples,
+ * column-major pixels.  Diffuse rays are final-evolved in place. */
+void o_continuum_shade(o_adray* rays, int64_t n_rays, const int32_t* hit_idx, const o_ftri* tris,
+                       const float* spectrum, const float* retina, int32_t n_lambda, int32_t upscale,
+                       const float* tex, int64_t tw, int64_t th, int64_t planes, const float* sky, int64_t sw,
+                       int64_t sh, int64_t height, int64_t width, float* rgb, float* tol);
+
 #ifdef __cplusplus
 }
 #endif

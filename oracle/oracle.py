@@ -33,6 +33,11 @@ class LambdaMode(C.Structure):
     _fields_ = [("mode", C.c_int32), ("n_strata", C.c_int32), ("lambda0", C.c_float), ("lambda1", C.c_float)]
 
 
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("look_at", C.c_float * 3), ("dir", C.c_float * 3), ("up", C.c_float * 3),
+                ("right", C.c_float * 3), ("fov_half_sin", C.c_float)]
+
+
 def build() -> str:
     subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
     return _LIB_PATH
@@ -79,6 +84,11 @@ def lib():
         L.o_trace_forward.argtypes = [vp, C.c_int64, C.POINTER(LambdaMode), C.c_uint64, f32p, C.c_int64, C.c_int64,
                                       C.c_int32, C.POINTER(Material), C.c_float, C.c_int, vp, C.c_int32, vp, vp,
                                       C.c_int32, C.c_int64, C.c_int64, C.c_int64, C.c_int64, vp, vp, C.c_int]
+        L.o_camera_look_at.argtypes = [f32p, f32p, f32p, C.c_double, C.POINTER(Camera)]
+        L.o_camera_rays.argtypes = [C.POINTER(Camera), C.c_int64, C.c_int64, C.c_float, C.c_uint64, rayp]
+        L.o_continuum_shade.argtypes = [rayp, C.c_int64, i32p, f32p, f32p, f32p, C.c_int32, C.c_int32, f32p,
+                                        C.c_int64, C.c_int64, C.c_int64, vp, C.c_int64, C.c_int64, C.c_int64,
+                                        C.c_int64, f32p, f32p]
         _lib = L
     return _lib
 
@@ -246,3 +256,114 @@ def trace_forward(wl, ray_begin: int = 0, ray_end: Optional[int] = None, nthread
         wl.frac_bits, wl.map_w, wl.map_h, ray_begin, ray_end, None if rays is None else rays.ctypes.data,
         stats.ctypes.data, nthreads)
     return tex, stats, rays
+
+
+# --------------------------------------------------------------------------- camera pass
+def camera_look_at(pos, look_at, up, fov: float) -> Camera:
+    """get_camera (src/geo.jl:183-191)."""
+    cam = Camera()
+    lib().o_camera_look_at(_v3(pos), _v3(look_at), _v3(up), float(fov), C.byref(cam))
+    return cam
+
+
+def camera_rays(cam: Camera, h: int, w: int, lam: float = 550.0, seed: int = 0) -> np.ndarray:
+    """wrap_ray_gen(camera_ray) over an h x w grid (src/ray_generators.jl:18-62)."""
+    out = np.zeros(h * w, dtype=T.ADRAY)
+    lib().o_camera_rays(C.byref(cam), h, w, float(lam), int(seed), out)
+    return out
+
+
+# The reference's retina curves (src/rgb_spectrum.jl:32-91) as knots
+# (nm, response); integers where the reference writes integers.
+RETINA_KNOTS = (
+    [(399, 0), (400, 0.0647036), (420, 0.147492), (438, 0.195683), (460, 0.162951), (466, 0), (534, 0),
+     (538, 0.243127), (571, 0.798209), (593, 0.980253), (602, 0.999977), (610, 0.98481), (660, 0.375838),
+     (680, 0.210109), (700, 0.11005)],
+    [(399, 0), (462, 0), (467, 0.165356), (474, 0.280228), (502, 0.587139), (521, 0.829692), (534, 0.924245),
+     (551, 0.910167), (572, 0.777366), (600, 0.372516), (609, 0.158767), (612, 0), (700, 0)],
+    [(399, 0), (413, 0.23889), (418, 0.291473), (437, 0.437376), (456, 0.590128), (463, 0.72815), (476, 0.581812),
+     (494, 0.452254), (515, 0.407615), (528, 0.299756), (536, 0), (608, 0), (611, 0.0407256), (614, 0.154091),
+     (620, 0.220637), (635, 0.225269), (667, 0.116114), (700, 0.0424846)],
+)
+
+
+def _piecewise_tree(points):
+    """The reference's `piecewise` (src/rgb_spectrum.jl:3-30) restated: a
+    binary tree of comparisons `lam < x_i` over 1-based knots, leaves
+    interpolating (y1 - y2) / (x1 - x2) * (lam - x1) + y1 with (x1, y1) the
+    upper knot of the segment."""
+    import math
+
+    def helper(lo, hi, i):
+        if hi - lo < 2:
+            raise ValueError("bad")
+        if hi - lo == 2:
+            (x1, y1), (x2, y2) = points[hi - 1], points[lo]
+            return ("leaf", x1, y1, x2, y2)
+        left = helper(lo, i, int(math.ceil((lo + i) / 2)))
+        right = helper(i - 1, hi, int(math.ceil((i + hi) / 2)))
+        return ("node", points[i - 1][0], left, right)
+
+    return helper(0, len(points), int(math.ceil(len(points) / 2)))
+
+
+def _piecewise_eval(tree, lam, f32: bool) -> float:
+    node = tree
+    while node[0] == "node":
+        node = node[2] if lam < node[1] else node[3]
+    _, x1, y1, x2, y2 = node
+    slope = (y1 - y2) / (x1 - x2)  # Python int / int -> float, float - int -> float, as Julia promotes
+    d = float(np.float32(lam) - np.float32(x1)) if f32 else float(lam - x1)
+    return float(slope) * d + y1
+
+
+def retina_factors(spectrum) -> np.ndarray:
+    """_spectrum_datastructs (src/rgb_spectrum.jl:135-149): [3, n] float32,
+    each curve over its sum at 400..700 nm (a left fold)."""
+    spec = np.asarray(spectrum, dtype=np.float32)
+    out = np.zeros((3, len(spec)), dtype=np.float32)
+    for c, knots in enumerate(RETINA_KNOTS):
+        tree = _piecewise_tree(knots)
+        norm = _piecewise_eval(tree, 400, False)
+        for x in range(401, 701):
+            norm = norm + _piecewise_eval(tree, x, False)
+        for i, lam in enumerate(spec):
+            out[c, i] = np.float32(_piecewise_eval(tree, np.float32(lam), True) / norm)
+    return out
+
+
+def continuum_shade(rays, hit_idx, tris, spectrum, retina, upscale, tex, sky, height, width):
+    """continuum_shade!(ExperimentalImager2) (src/ray_imagers.jl:383-503) with
+    an exact-weight model of the texture filter.  tex: float32 [w, h, planes]
+    (Fortran order), sky: float32 [sw, sh, 3] or None.  Returns (rgb, tol,
+    rays): rgb and tol [height, width, 3] per pixel (row, col), rays with the
+    diffuse ones final-evolved."""
+    rays = rays.copy()
+    spec = np.ascontiguousarray(spectrum, np.float32)
+    ret = np.ascontiguousarray(retina, np.float32).reshape(3, len(spec))
+    texf = np.ascontiguousarray(np.asarray(tex, np.float32).ravel(order="F"))
+    tw, th, tp = tex.shape
+    if sky is not None:
+        skyf = np.ascontiguousarray(np.asarray(sky, np.float32).ravel(order="F"))
+        sw, sh = sky.shape[0], sky.shape[1]
+    else:
+        skyf, sw, sh = None, 0, 0
+    rgb = np.zeros(height * width * 3, np.float32)
+    tol = np.zeros(height * width * 3, np.float32)
+    tris = np.ascontiguousarray(tris, np.float32)
+    lib().o_continuum_shade(rays, len(rays), np.ascontiguousarray(hit_idx, np.int32), tris, spec, ret.ravel(),
+                            len(spec), upscale, texf, tw, th, tp, None if skyf is None else skyf.ctypes.data, sw, sh,
+                            height, width, rgb, tol)
+    img = rgb.reshape(width, height, 3).transpose(1, 0, 2)
+    tl = tol.reshape(width, height, 3).transpose(1, 0, 2)
+    return img, tl, rays
+
+
+def render_camera(tris, first_diffuse, cam, height, width, upscale, depth, mat, spectrum, retina, tex, sky,
+                  seed=0, lam=550.0, force_rand=None, quirks=True, nthreads=0):
+    """The camera pass: camera_rays -> run_evolution! -> continuum_shade!."""
+    h, w = height // upscale, width // upscale
+    rays = camera_rays(cam, h, w, lam, seed)
+    rays, hit = run_evolution(rays, tris, depth, first_diffuse, mat, force_rand=force_rand, seed=seed,
+                              quirks=quirks, nthreads=nthreads)
+    return continuum_shade(rays, hit, tris, spectrum, retina, upscale, tex, sky, height, width)

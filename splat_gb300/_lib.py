@@ -72,6 +72,20 @@ class SceneInfo(C.Structure):
                 ("bvh_pad", C.c_float)]
 
 
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("look_at", C.c_float * 3), ("dir", C.c_float * 3), ("up", C.c_float * 3),
+                ("right", C.c_float * 3), ("fov_half_sin", C.c_float)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [
+        ("camera", Camera), ("height", C.c_int64), ("width", C.c_int64), ("upscale", C.c_int64),
+        ("seed", C.c_uint64), ("depth", C.c_int32), ("hitter", C.c_int32), ("material", Material),
+        ("force_rand", C.c_float), ("flags", C.c_uint32), ("lambda_", C.c_float), ("n_lambda", C.c_int32),
+        ("spectrum", C.c_float * MAX_LAMBDA), ("retina", (C.c_float * MAX_LAMBDA) * 3),
+    ]
+
+
 # every symbol the header declares, with its ctypes signature
 vp = C.c_void_p
 i32, i64, u32, u64, f32, sz = C.c_int32, C.c_int64, C.c_uint32, C.c_uint64, C.c_float, C.c_size_t
@@ -94,6 +108,17 @@ SIGNATURES = {
     "splat_trace_workspace_size": ([i64], sz),
     "splat_trace_forward": ([vp, C.POINTER(TraceParams), vp, vp, sz, vp, vp], i32),
     "splat_trace_forward_host": ([vp, vp, C.POINTER(TraceParams), vp, vp, vp, sz, C.POINTER(TraceStats), vp], i32),
+    "splat_camera_look_at": ([vp, vp, vp, C.c_double, C.POINTER(Camera)], i32),
+    "splat_camera_rays": ([C.POINTER(Camera), i64, i64, f32, u64, vp, vp], i32),
+    "splat_retina_factors": ([vp, i32, vp], i32),
+    "splat_shader_create": ([i64, i64, i32, i64, i64, vp], i32),
+    "splat_shader_destroy": ([vp], i32),
+    "splat_shader_set_light_map": ([vp, vp, i32, i32, vp], i32),
+    "splat_shader_set_skydome": ([vp, vp, vp], i32),
+    "splat_continuum_shade": ([vp, vp, vp, i64, vp, vp, vp, i32, i64, i64, i64, vp, vp], i32),
+    "splat_render_workspace_size": ([i64], sz),
+    "splat_render_camera": ([vp, vp, C.POINTER(RenderParams), vp, vp, sz, vp], i32),
+    "splat_image_accumulate": ([vp, vp, i64, i32, vp], i32),
     "splat_batch_device_bytes": ([i32, i64], sz),
     "splat_batch_create": ([i32, i64, vp], i32),
     "splat_batch_destroy": ([vp], i32),
@@ -116,6 +141,7 @@ TUNE_BRUTE_BLOCKS_PER_SM = 0
 TUNE_BVH_BLOCKS_PER_SM = 1
 TUNE_EVOLVE_BLOCKS_PER_SM = 2
 TUNE_SPLAT_BLOCKS_PER_SM = 3
+TUNE_SPLAT_AGGREGATE = 4
 
 KERNEL_GENERATE = 0
 KERNEL_HIT_BRUTE = 1
@@ -124,7 +150,8 @@ KERNEL_EVOLVE = 3
 KERNEL_AUX = 4
 KERNEL_SPLAT = 5
 KERNEL_BATCH = 6
-KERNEL_ALL = 7
+KERNEL_SHADE = 7
+KERNEL_ALL = 8
 
 _lib = None
 _lock = threading.Lock()

@@ -29,6 +29,7 @@ KNOB_CHOICES = {
     L.TUNE_BVH_BLOCKS_PER_SM: (4, 8, 16, 32),
     L.TUNE_EVOLVE_BLOCKS_PER_SM: (4, 8, 16),
     L.TUNE_SPLAT_BLOCKS_PER_SM: (4, 8, 16),
+    L.TUNE_SPLAT_AGGREGATE: (0, 1),
 }
 
 

@@ -687,7 +687,11 @@ splat_status_t splat_trace_forward_host(splat_scene_t* scene, const splat_ftri_t
 
 splat_status_t splat_set_tuning(int32_t key, int32_t value) {
     if (key < 0 || key >= SPLAT_TUNE_KEYS) return fail(SPLAT_ERR_INVALID, "set_tuning: unknown key");
-    if (value < 1 || value > 256) return fail(SPLAT_ERR_INVALID, "set_tuning: value must be 1..256");
+    if (key == SPLAT_TUNE_SPLAT_AGGREGATE) {
+        if (value != 0 && value != 1) return fail(SPLAT_ERR_INVALID, "set_tuning: aggregate must be 0 or 1");
+    } else if (value < 1 || value > 256) {
+        return fail(SPLAT_ERR_INVALID, "set_tuning: value must be 1..256");
+    }
     g_tune[key] = value;
     return SPLAT_OK;
 }
@@ -1102,3 +1106,411 @@ splat_status_t splat_batch_replay(splat_batch_t* b, const uint64_t* seeds, int32
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// camera pass
+// ---------------------------------------------------------------------------
+namespace {
+
+// Retina response curves of src/rgb_spectrum.jl:32-91 (the reference's
+// `piecewise` knots, nm -> response): the table has to be the same for the
+// shading to match.  piecewise() interpolates linearly on the segment whose
+// left knot is the last one <= lambda (first / last segment outside the
+// knots), as (y1 - y0) / (x1 - x0) * (lambda - x1) + y1 in double with the
+// difference lambda - x1 taken in the argument's own type.
+struct Knot {
+    int x;
+    double y;
+};
+const Knot kRetinaRed[] = {{399, 0},         {400, 0.0647036}, {420, 0.147492}, {438, 0.195683}, {460, 0.162951},
+                           {466, 0},         {534, 0},         {538, 0.243127}, {571, 0.798209}, {593, 0.980253},
+                           {602, 0.999977},  {610, 0.98481},   {660, 0.375838}, {680, 0.210109}, {700, 0.11005}};
+const Knot kRetinaGreen[] = {{399, 0},        {462, 0},        {467, 0.165356}, {474, 0.280228}, {502, 0.587139},
+                             {521, 0.829692}, {534, 0.924245}, {551, 0.910167}, {572, 0.777366}, {600, 0.372516},
+                             {609, 0.158767}, {612, 0},        {700, 0}};
+const Knot kRetinaBlue[] = {{399, 0},         {413, 0.23889},  {418, 0.291473}, {437, 0.437376}, {456, 0.590128},
+                            {463, 0.72815},   {476, 0.581812}, {494, 0.452254}, {515, 0.407615}, {528, 0.299756},
+                            {536, 0},         {608, 0},        {611, 0.0407256}, {614, 0.154091}, {620, 0.220637},
+                            {635, 0.225269},  {667, 0.116114}, {700, 0.0424846}};
+
+template <int N>
+int segment_of(const Knot (&k)[N], double lam) {
+    int s = 0;
+    while (s + 2 < N && !(lam < (double)k[s + 1].x)) ++s;
+    return s;
+}
+
+// Float32 argument (a spectrum wavelength): lambda - x1 in float.
+template <int N>
+double piecewise_f(const Knot (&k)[N], float lam) {
+    const int s = segment_of(k, (double)lam);
+    const double slope = (k[s + 1].y - k[s].y) / (double)(k[s + 1].x - k[s].x);
+    const float d = lam - (float)k[s + 1].x;
+    return slope * (double)d + k[s + 1].y;
+}
+
+// Integer argument (the normalisers' 400:700 sweep): lambda - x1 exact.
+template <int N>
+double piecewise_i(const Knot (&k)[N], int lam) {
+    const int s = segment_of(k, (double)lam);
+    const double slope = (k[s + 1].y - k[s].y) / (double)(k[s + 1].x - k[s].x);
+    return slope * (double)(lam - k[s + 1].x) + k[s + 1].y;
+}
+
+// sum(f(x) for x = 400:700): a left fold.
+template <int N>
+double retina_norm(const Knot (&k)[N]) {
+    double s = piecewise_i(k, 400);
+    for (int x = 401; x <= 700; ++x) s = s + piecewise_i(k, x);
+    return s;
+}
+
+}  // namespace
+
+struct splat_shader {
+    int device = 0;
+    int64_t map_w = 0, map_h = 0, sky_w = 0, sky_h = 0;
+    int32_t planes = 0;
+    cudaArray_t map_arr = nullptr, sky_arr = nullptr;
+    cudaTextureObject_t map_tex = 0, sky_tex = 0;
+    cudaSurfaceObject_t map_surf = 0;
+};
+
+namespace {
+
+void shader_free(splat_shader* s) {
+    if (!s) return;
+    if (s->map_tex) cudaDestroyTextureObject(s->map_tex);
+    if (s->sky_tex) cudaDestroyTextureObject(s->sky_tex);
+    if (s->map_surf) cudaDestroySurfaceObject(s->map_surf);
+    if (s->map_arr) cudaFreeArray(s->map_arr);
+    if (s->sky_arr) cudaFreeArray(s->sky_arr);
+    delete s;
+}
+
+// CuTexture(CuTextureArray(a); interpolation = LinearInterpolation()):
+// float elements, linear filter, clamp addressing, unnormalised coordinates.
+cudaError_t make_texture(cudaArray_t arr, cudaTextureObject_t* tex) {
+    cudaResourceDesc rd;
+    std::memset(&rd, 0, sizeof(rd));
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = arr;
+    cudaTextureDesc td;
+    std::memset(&td, 0, sizeof(td));
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 0;
+    return cudaCreateTextureObject(tex, &rd, &td, nullptr);
+}
+
+cudaError_t copy_to_array(const void* src, int64_t w, int64_t h, int64_t d, cudaArray_t arr, cudaStream_t st) {
+    cudaMemcpy3DParms p;
+    std::memset(&p, 0, sizeof(p));
+    p.srcPtr = make_cudaPitchedPtr(const_cast<void*>(src), (size_t)w * 4, (size_t)w, (size_t)h);
+    p.dstArray = arr;
+    p.extent = make_cudaExtent((size_t)w, (size_t)h, (size_t)d);
+    p.kind = cudaMemcpyDeviceToDevice;
+    return cudaMemcpy3DAsync(&p, st);
+}
+
+bool camera_ok(const splat_camera_t* c) {
+    if (!c) return false;
+    const float* v[5] = {c->pos, c->look_at, c->dir, c->up, c->right};
+    for (auto p : v)
+        for (int i = 0; i < 3; ++i)
+            if (!std::isfinite(p[i])) return false;
+    return std::isfinite(c->fov_half_sin) && c->fov_half_sin > 0.0f;
+}
+
+CameraParams camera_params(const splat_camera_t* cam, int64_t h, int64_t w, float lambda, uint64_t seed) {
+    CameraParams c;
+    std::memset(&c, 0, sizeof(c));
+    c.cam = *cam;
+    c.h = h;
+    c.w = w;
+    c.seed = seed;
+    c.lambda = lambda;
+    c.cos45 = 1.0 / std::sqrt(2.0);
+    return c;
+}
+
+ShadeParams shade_params(const splat_shader* sh, const float* spectrum, const float* retina, int32_t n_lambda,
+                         int64_t upscale, int64_t height, float* rgb, int32_t retina_stride) {
+    ShadeParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.map_tex = sh->map_tex;
+    p.sky_tex = sh->sky_tex;
+    p.map_w = sh->map_w;
+    p.map_h = sh->map_h;
+    p.sky_w = sh->sky_w;
+    p.sky_h = sh->sky_h;
+    p.has_sky = sh->sky_arr ? 1 : 0;
+    p.n_lambda = n_lambda;
+    p.nd = (int32_t)upscale;
+    p.cam_h = height / upscale;
+    p.height = height;
+    p.rgb = rgb;
+    // upres(N), src/alg_types.jl:108
+    for (int k = 1; k <= p.nd; ++k)
+        p.deltas[k - 1] = ((float)k / (float)p.nd - 0.5f) - (1.0f / (2.0f * (float)p.nd));
+    for (int i = 0; i < n_lambda; ++i) {
+        p.spectrum[i] = spectrum[i];
+        for (int c = 0; c < 3; ++c) p.retina[c][i] = retina[(size_t)c * retina_stride + i];
+    }
+    return p;
+}
+
+splat_status_t check_image(int64_t height, int64_t width, int64_t upscale) {
+    if (upscale < 1 || upscale > 16) return fail(SPLAT_ERR_INVALID, "upscale must be 1..16");
+    if (height < upscale || width < upscale || height % upscale || width % upscale)
+        return fail(SPLAT_ERR_INVALID, "image size must be a positive multiple of upscale");
+    if ((height / upscale) * (width / upscale) >= (int64_t(1) << 32))
+        return fail(SPLAT_ERR_INVALID, "more than 2^32 camera rays");
+    return SPLAT_OK;
+}
+
+}  // namespace
+
+splat_status_t splat_camera_look_at(const float pos[3], const float look_at[3], const float true_up[3], double fov,
+                                    splat_camera_t* out) {
+    if (!pos || !look_at || !true_up || !out) return fail(SPLAT_ERR_INVALID, "camera_look_at: null pointer");
+    if (!(fov > 0.0) || !(fov < 2.0 * M_PI)) return fail(SPLAT_ERR_INVALID, "camera_look_at: fov must be in (0, 2 pi)");
+    auto sub = [](const float* a, const float* b, float* o) {
+        for (int i = 0; i < 3; ++i) o[i] = a[i] - b[i];
+    };
+    auto cross = [](const float* a, const float* b, float* o) {
+        o[0] = a[1] * b[2] - a[2] * b[1];
+        o[1] = a[2] * b[0] - a[0] * b[2];
+        o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    auto normalize = [](float* v) {
+        const float inv = 1.0f / std::sqrt((v[0] * v[0] + v[1] * v[1]) + v[2] * v[2]);
+        for (int i = 0; i < 3; ++i) v[i] = v[i] * inv;
+    };
+    splat_camera_t c;
+    std::memset(&c, 0, sizeof(c));
+    for (int i = 0; i < 3; ++i) {
+        c.pos[i] = pos[i];
+        c.look_at[i] = look_at[i];
+    }
+    sub(look_at, pos, c.dir);
+    normalize(c.dir);
+    cross(c.dir, true_up, c.right);
+    normalize(c.right);
+    cross(c.right, c.dir, c.up);
+    normalize(c.up);
+    c.fov_half_sin = (float)std::sin(fov / 2.0);
+    if (!camera_ok(&c)) return fail(SPLAT_ERR_INVALID, "camera_look_at: degenerate camera (up parallel to view?)");
+    *out = c;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_camera_rays(const splat_camera_t* camera, int64_t height, int64_t width, float lambda,
+                                 uint64_t seed, splat_adray_t* d_rays, void* stream) {
+    if (!camera_ok(camera)) return fail(SPLAT_ERR_INVALID, "camera_rays: bad camera");
+    if (height < 1 || width < 1 || height * width >= (int64_t(1) << 32))
+        return fail(SPLAT_ERR_INVALID, "camera_rays: bad grid size");
+    if (!d_rays) return fail(SPLAT_ERR_INVALID, "camera_rays: null output");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    ProfScope ps(SPLAT_KERNEL_SHADE, st);
+    SPLAT_CUDA(launch_camera_aos(camera_params(camera, height, width, lambda, seed), height * width, d_rays,
+                                 sm_count_current(), st),
+               "camera rays");
+    return SPLAT_OK;
+}
+
+splat_status_t splat_retina_factors(const float* spectrum, int32_t n_lambda, float* out) {
+    if (n_lambda < 0 || (n_lambda > 0 && (!spectrum || !out))) return fail(SPLAT_ERR_INVALID, "retina_factors: bad arguments");
+    const double r0 = retina_norm(kRetinaRed), g0 = retina_norm(kRetinaGreen), b0 = retina_norm(kRetinaBlue);
+    for (int32_t i = 0; i < n_lambda; ++i) {
+        out[i] = (float)(piecewise_f(kRetinaRed, spectrum[i]) / r0);
+        out[n_lambda + i] = (float)(piecewise_f(kRetinaGreen, spectrum[i]) / g0);
+        out[2 * n_lambda + i] = (float)(piecewise_f(kRetinaBlue, spectrum[i]) / b0);
+    }
+    return SPLAT_OK;
+}
+
+splat_status_t splat_shader_create(int64_t map_w, int64_t map_h, int32_t n_planes, int64_t sky_w, int64_t sky_h,
+                                   splat_shader_t** out) {
+    if (!out) return fail(SPLAT_ERR_INVALID, "shader_create: null output");
+    *out = nullptr;
+    cudaDeviceProp prop;
+    int dev = 0;
+    SPLAT_CUDA(cudaGetDevice(&dev), "shader_create: device");
+    SPLAT_CUDA(cudaGetDeviceProperties(&prop, dev), "shader_create: properties");
+    const int64_t lim = prop.maxTexture3D[0];
+    if (map_w < 1 || map_h < 1 || n_planes < 1 || n_planes > SPLAT_MAX_LAMBDA || map_w > lim ||
+        map_h > prop.maxTexture3D[1])
+        return fail(SPLAT_ERR_INVALID, "shader_create: light map size outside the 3-D texture limits");
+    if (sky_w < 0 || sky_h < 0 || (sky_w > 0) != (sky_h > 0) || sky_w > lim || sky_h > prop.maxTexture3D[1])
+        return fail(SPLAT_ERR_INVALID, "shader_create: bad skydome size");
+    splat_shader* s = new (std::nothrow) splat_shader();
+    if (!s) return fail(SPLAT_ERR_ALLOC, "shader_create: host allocation");
+    s->device = dev;
+    s->map_w = map_w;
+    s->map_h = map_h;
+    s->planes = n_planes;
+    s->sky_w = sky_w;
+    s->sky_h = sky_h;
+    const cudaChannelFormatDesc fd = cudaCreateChannelDesc<float>();
+    cudaError_t e = cudaMalloc3DArray(&s->map_arr, &fd, make_cudaExtent((size_t)map_w, (size_t)map_h, (size_t)n_planes),
+                                      cudaArraySurfaceLoadStore);
+    if (e == cudaSuccess) e = make_texture(s->map_arr, &s->map_tex);
+    if (e == cudaSuccess) {
+        cudaResourceDesc rd;
+        std::memset(&rd, 0, sizeof(rd));
+        rd.resType = cudaResourceTypeArray;
+        rd.res.array.array = s->map_arr;
+        e = cudaCreateSurfaceObject(&s->map_surf, &rd);
+    }
+    if (e == cudaSuccess && sky_w > 0) {
+        e = cudaMalloc3DArray(&s->sky_arr, &fd, make_cudaExtent((size_t)sky_w, (size_t)sky_h, 3), 0);
+        if (e == cudaSuccess) e = make_texture(s->sky_arr, &s->sky_tex);
+    }
+    if (e != cudaSuccess) {
+        shader_free(s);
+        return cuda_fail(e, "shader_create: texture arrays");
+    }
+    *out = s;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_shader_destroy(splat_shader_t* shader) {
+    shader_free(shader);
+    return SPLAT_OK;
+}
+
+splat_status_t splat_shader_set_light_map(splat_shader_t* sh, const void* d_map, int32_t accum, int32_t frac_bits,
+                                          void* stream) {
+    if (!sh || !d_map) return fail(SPLAT_ERR_INVALID, "shader_set_light_map: null argument");
+    if (frac_bits < 0 || frac_bits > 30) return fail(SPLAT_ERR_INVALID, "shader_set_light_map: frac_bits must be 0..30");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    ProfScope ps(SPLAT_KERNEL_SHADE, st);
+    if (accum == SPLAT_ACCUM_F32) {
+        SPLAT_CUDA(copy_to_array(d_map, sh->map_w, sh->map_h, sh->planes, sh->map_arr, st), "light map -> array");
+    } else if (accum == SPLAT_ACCUM_I32) {
+        SPLAT_CUDA(launch_map_to_array(reinterpret_cast<const int32_t*>(d_map), sh->map_w, sh->map_h, sh->planes,
+                                       std::ldexp(1.0f, -frac_bits), sh->map_surf, sm_count_current(), st),
+                   "light map -> array");
+    } else {
+        return fail(SPLAT_ERR_INVALID, "shader_set_light_map: unknown accumulation");
+    }
+    return SPLAT_OK;
+}
+
+splat_status_t splat_shader_set_skydome(splat_shader_t* sh, const float* d_sky, void* stream) {
+    if (!sh || !d_sky) return fail(SPLAT_ERR_INVALID, "shader_set_skydome: null argument");
+    if (!sh->sky_arr) return fail(SPLAT_ERR_INVALID, "shader_set_skydome: shader created without a skydome");
+    SPLAT_CUDA(copy_to_array(d_sky, sh->sky_w, sh->sky_h, 3, sh->sky_arr, reinterpret_cast<cudaStream_t>(stream)),
+               "skydome -> array");
+    return SPLAT_OK;
+}
+
+splat_status_t splat_continuum_shade(const splat_scene_t* scene, const splat_shader_t* shader, splat_adray_t* d_rays,
+                                     int64_t n_rays, const int32_t* d_hit_idx, const float* spectrum,
+                                     const float* retina, int32_t n_lambda, int64_t upscale, int64_t height,
+                                     int64_t width, float* d_rgb, void* stream) {
+    if (!scene || !shader) return fail(SPLAT_ERR_INVALID, "continuum_shade: null scene or shader");
+    splat_status_t rc = check_image(height, width, upscale);
+    if (rc != SPLAT_OK) return rc;
+    if (n_rays != (height / upscale) * (width / upscale))
+        return fail(SPLAT_ERR_INVALID, "continuum_shade: n_rays must be (height / upscale) * (width / upscale)");
+    if (n_lambda < 1 || n_lambda > shader->planes || !spectrum || !retina)
+        return fail(SPLAT_ERR_INVALID, "continuum_shade: spectrum must have 1..planes wavelengths");
+    if (!d_rays || !d_hit_idx || !d_rgb) return fail(SPLAT_ERR_INVALID, "continuum_shade: null pointer");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const ShadeParams p = shade_params(shader, spectrum, retina, n_lambda, upscale, height, d_rgb, n_lambda);
+    ProfScope ps(SPLAT_KERNEL_SHADE, st);
+    SPLAT_CUDA(launch_shade_aos(d_rays, n_rays, d_hit_idx, scene->d_ftri, scene->n_tris, scene->d_err, p,
+                                sm_count_current(), st),
+               "continuum_shade");
+    return SPLAT_OK;
+}
+
+size_t splat_render_workspace_size(int64_t n_camera_rays) {
+    return n_camera_rays <= 0 ? kAlign : work_bytes(n_camera_rays) + soa_bytes(n_camera_rays) + kAlign;
+}
+
+splat_status_t splat_render_camera(const splat_scene_t* scene, const splat_shader_t* shader,
+                                   const splat_render_params_t* P, float* d_rgb, void* d_workspace,
+                                   size_t workspace_bytes, void* stream) {
+    if (!scene || !shader || !P) return fail(SPLAT_ERR_INVALID, "render_camera: null argument");
+    if (!camera_ok(&P->camera)) return fail(SPLAT_ERR_INVALID, "render_camera: bad camera");
+    splat_status_t rc = check_image(P->height, P->width, P->upscale);
+    if (rc != SPLAT_OK) return rc;
+    if (P->depth < 1 || P->depth > 8) return fail(SPLAT_ERR_INVALID, "render_camera: depth must be 1..8");
+    if (!valid_material(&P->material)) return fail(SPLAT_ERR_INVALID, "render_camera: bad material");
+    if (P->n_lambda < 1 || P->n_lambda > shader->planes)
+        return fail(SPLAT_ERR_INVALID, "render_camera: n_lambda must be 1..planes of the shader's map");
+    if ((P->hitter == SPLAT_HITTER_BVH || P->hitter == SPLAT_HITTER_BVH2) && !scene->d_nodes && scene->n_recs > 0)
+        return fail(SPLAT_ERR_INVALID, "render_camera: BVH hitter on a scene without BVH");
+    if (!d_rgb) return fail(SPLAT_ERR_INVALID, "render_camera: null image");
+    const int64_t ch = P->height / P->upscale, cw = P->width / P->upscale;
+    const int64_t cnt = ch * cw;
+    if (!d_workspace || workspace_bytes < splat_render_workspace_size(cnt))
+        return fail(SPLAT_ERR_WORKSPACE, "render_camera: workspace smaller than splat_render_workspace_size");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int sm = sm_count_current();
+    Work w = carve_work(d_workspace, cnt);
+    char* p = reinterpret_cast<char*>(w.counts) + kCounterBytes;
+    p = reinterpret_cast<char*>(align_up(reinterpret_cast<size_t>(p)));
+    const RaySoA sky = carve_soa(p, cnt);
+    int64_t* sky_count = &w.counts[kSplatCount + 1];
+    SPLAT_CUDA(cudaMemsetAsync(w.counts, 0, kCounterBytes, st), "memset counters");
+    SPLAT_CUDA(cudaMemsetAsync(d_rgb, 0, (size_t)P->height * P->width * 3 * sizeof(float), st), "clear image");
+    {
+        ProfScope ps(SPLAT_KERNEL_SHADE, st);
+        SPLAT_CUDA(launch_camera_soa(camera_params(&P->camera, ch, cw, P->lambda, P->seed), cnt, w.a, &w.counts[0],
+                                     sm, st),
+                   "camera rays");
+    }
+    EvolveArgs ea;
+    std::memset(&ea, 0, sizeof(ea));
+    ea.tris = scene->d_ftri;
+    ea.n_tris = scene->n_tris;
+    ea.err = scene->d_err;
+    ea.first_diffuse = scene->first_diffuse;
+    ea.material = P->material;
+    ea.seed = P->seed;
+    ea.force_rand = P->force_rand;
+    ea.quirks = (P->flags & SPLAT_FLAG_REF_QUIRKS) ? 1 : 0;
+    ea.splat_q = w.q;
+    ea.splat_count = &w.counts[kSplatCount];
+    ea.sky_q = sky;
+    ea.sky_count = sky_count;
+    RaySoA cur = w.a, nxt = w.b;
+    for (int32_t b = 1; b <= P->depth; ++b) {
+        RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0};
+        rc = hit_any(scene, P->hitter, src, cnt, w.hit, nullptr, w.tmp, st);
+        if (rc != SPLAT_OK) return rc;
+        ea.in = cur;
+        ea.out = nxt;
+        ea.in_count = &w.counts[b - 1];
+        ea.out_count = &w.counts[b];
+        ea.hit_idx = w.hit;
+        ea.bounce = (uint32_t)b;
+        ea.last = b == P->depth ? 1 : 0;
+        {
+            ProfScope ps(SPLAT_KERNEL_EVOLVE, st);
+            SPLAT_CUDA(launch_evolve_camera(ea, cnt, sm, st), "evolve");
+        }
+        std::swap(cur, nxt);
+    }
+    const ShadeParams sp =
+        shade_params(shader, P->spectrum, &P->retina[0][0], P->n_lambda, P->upscale, P->height, d_rgb, SPLAT_MAX_LAMBDA);
+    ProfScope ps(SPLAT_KERNEL_SHADE, st);
+    SPLAT_CUDA(launch_shade_queues(w.q, &w.counts[kSplatCount], sky, sky_count, scene->d_ftri, sp, cnt, sm, st),
+               "shade");
+    return SPLAT_OK;
+}
+
+splat_status_t splat_image_accumulate(float* d_out, const float* d_rgb, int64_t n, int32_t iteration, void* stream) {
+    if (n < 0 || iteration < 1) return fail(SPLAT_ERR_INVALID, "image_accumulate: bad size or iteration");
+    if (n == 0) return SPLAT_OK;
+    if (!d_out || !d_rgb) return fail(SPLAT_ERR_INVALID, "image_accumulate: null pointer");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    ProfScope ps(SPLAT_KERNEL_SHADE, st);
+    SPLAT_CUDA(launch_image_accumulate(d_out, d_rgb, n, iteration, sm_count_current(), st), "image_accumulate");
+    return SPLAT_OK;
+}

@@ -200,6 +200,45 @@ __global__ void __launch_bounds__(256, 3) batch_splat_kernel(RaySoA q, const int
     }
 }
 
+// The same through the block's shared texel table keyed by texel address
+// (rays of one block may splat into different items' maps): plane by plane
+// up to the block's largest plane count.
+__global__ void __launch_bounds__(256, 3) batch_splat_agg_kernel(RaySoA q, const int64_t* __restrict__ count,
+                                                                 const BatchItem* __restrict__ items) {
+    __shared__ unsigned long long s_key[kAggSlots];
+    __shared__ int32_t s_val[kAggSlots];
+    __shared__ int s_planes;
+    const int64_t n = *count;
+    addr_table_clear(s_key, s_val);
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = base + threadIdx.x;
+        const bool live = k < n;
+        if (threadIdx.x == 0) s_planes = 0;
+        __syncthreads();
+        RayState r;
+        Tri T;
+        TriUV quv;
+        const BatchItem* it = nullptr;
+        int planes = 0;
+        if (live) {
+            r = load_ray(q, k);
+            it = &items[q.id[k] >> kSlotShift];
+            planes = it->sp.n_lambda > 0 ? it->sp.n_lambda : 1;
+            T = load_tri(it->ftri, r.ignore);
+            quv = tri_uv(T);
+            atomicMax(&s_planes, planes);
+        }
+        __syncthreads();
+        const int block_planes = s_planes;
+        for (int il = 0; il < block_planes; ++il) {
+            if (il < planes) (void)splat_ray_plane(it->sp, r, T, quv, il, AddrTableSink{it->sp, s_key, s_val});
+            __syncthreads();
+            addr_table_flush(s_key, s_val);
+            __syncthreads();
+        }
+    }
+}
+
 static int grid_cap(int64_t n, int threads, int sm_count, int per_sm) {
     int64_t b = (n + threads - 1) / threads;
     const int64_t cap = (int64_t)sm_count * per_sm;
@@ -226,7 +265,11 @@ cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s) {
         batch_evolve_kernel<<<grid_cap(a.cap_rays, kBatchThreads, a.sm_count, 8), kBatchThreads, 0, s>>>(
             a.cur, a.next, a.queue, a.cur_count, a.next_count, a.queue_count, items, a.tick, a.hit_idx, a.err);
         ++g_launches;
-        batch_splat_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count, items);
+        if (g_tune[SPLAT_TUNE_SPLAT_AGGREGATE])
+            batch_splat_agg_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count,
+                                                                                           items);
+        else
+            batch_splat_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count, items);
         ++g_launches;
     }
     return cudaGetLastError();

@@ -137,18 +137,24 @@ __device__ __forceinline__ void add_stats(splat_trace_stats_t* st, int diffuse, 
 // TRACE: diffuse rays are final-evolved and splatted here, misses dropped, the
 // last bounce skips the optics.  PLUGIN: retired rays are written back to the
 // caller's AoS array with their status, as run_evolution! leaves them.
-template <bool TRACE>
+// MODE 0: plugin (retired rays written back to the caller's AoS array);
+// 1: trace (diffuse rays final-evolved into the splat queue, escaped rays
+// dropped); 2: camera (as trace, escaped rays queued unchanged for the sky).
+template <int MODE>
 __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
+    constexpr bool TRACE = MODE != 0;
+    constexpr bool SKY = MODE == 2;
     __shared__ int s_warp[kEvolveThreads / 32];
     __shared__ int s_wdif[kEvolveThreads / 32];
-    __shared__ unsigned long long s_base, s_dbase;
+    __shared__ int s_wsky[kEvolveThreads / 32];
+    __shared__ unsigned long long s_base, s_dbase, s_sbase;
     const int64_t n = *A.in_count;
     const int lane = lane_id();
     const int wid = threadIdx.x >> 5;
     const bool quirks = A.quirks != 0;
     for (int64_t base = (int64_t)blockIdx.x * kEvolveThreads; base < n; base += (int64_t)gridDim.x * kEvolveThreads) {
         const int64_t k = base + threadIdx.x;
-        bool keep = false, dif = false;
+        bool keep = false, dif = false, sky = false;
         RayState r, o;
         uint32_t id = 0;
         int32_t ih = 1;
@@ -160,30 +166,39 @@ __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
             const int fate = evolve_one<TRACE>(r, A.hit_idx[k], id, v, o, ih);
             keep = fate == kFateKeep;
             dif = fate == kFateDiffuse;
+            sky = SKY && fate == kFateInfinity;
             if (!TRACE && fate == kFateDiffuse) ray_to_aos(A.aos[id], r, kStatusDiffuse);
             if (!TRACE && fate == kFateInfinity) ray_to_aos(A.aos[id], r, kStatusInfinity);
         }
         // compaction of the survivors (and, tracing, of the diffuse rays into
-        // the splat queue): ballot -> block scan -> one atomic per block each
+        // the splat queue and of the escaped ones into the sky queue): ballot
+        // -> block scan -> one atomic per block and queue
         const unsigned kb = __ballot_sync(kFull, keep);
         const unsigned db = TRACE ? __ballot_sync(kFull, dif) : 0u;
+        const unsigned sb = SKY ? __ballot_sync(kFull, sky) : 0u;
         if (lane == 0) {
             s_warp[wid] = __popc(kb);
             s_wdif[wid] = __popc(db);
+            s_wsky[wid] = __popc(sb);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            int tot = 0, dtot = 0;
+            int tot = 0, dtot = 0, stot = 0;
             for (int w = 0; w < kEvolveThreads / 32; ++w) {
-                const int c = s_warp[w], d = s_wdif[w];
+                const int c = s_warp[w], d = s_wdif[w], e = s_wsky[w];
                 s_warp[w] = tot;
                 s_wdif[w] = dtot;
+                s_wsky[w] = stot;
                 tot += c;
                 dtot += d;
+                stot += e;
             }
             s_base = tot ? atomicAdd(reinterpret_cast<unsigned long long*>(A.out_count), (unsigned long long)tot) : 0ull;
             s_dbase = dtot ? atomicAdd(reinterpret_cast<unsigned long long*>(A.splat_count), (unsigned long long)dtot)
                            : 0ull;
+            if (SKY)
+                s_sbase = stot ? atomicAdd(reinterpret_cast<unsigned long long*>(A.sky_count), (unsigned long long)stot)
+                               : 0ull;
         }
         __syncthreads();
         const unsigned below = (1u << lane) - 1u;
@@ -191,6 +206,8 @@ __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
             store_ray(A.out, (int64_t)s_base + s_warp[wid] + __popc(kb & below), o, id);
         } else if (TRACE && dif) {
             store_ray(A.splat_q, (int64_t)s_dbase + s_wdif[wid] + __popc(db & below), o, id);
+        } else if (SKY && sky) {
+            store_ray(A.sky_q, (int64_t)s_sbase + s_wsky[wid] + __popc(sb & below), r, id);
         }
         __syncthreads();
     }
@@ -205,14 +222,21 @@ static int evolve_grid(int64_t cap, int sm_count) {
 
 cudaError_t launch_evolve_trace(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s) {
     if (cap <= 0) return cudaSuccess;
-    evolve_kernel<true><<<evolve_grid(cap, sm_count), kEvolveThreads, 0, s>>>(a);
+    evolve_kernel<1><<<evolve_grid(cap, sm_count), kEvolveThreads, 0, s>>>(a);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_evolve_camera(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s) {
+    if (cap <= 0) return cudaSuccess;
+    evolve_kernel<2><<<evolve_grid(cap, sm_count), kEvolveThreads, 0, s>>>(a);
     ++g_launches;
     return cudaGetLastError();
 }
 
 cudaError_t launch_evolve_plugin(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s) {
     if (cap <= 0) return cudaSuccess;
-    evolve_kernel<false><<<evolve_grid(cap, sm_count), kEvolveThreads, 0, s>>>(a);
+    evolve_kernel<0><<<evolve_grid(cap, sm_count), kEvolveThreads, 0, s>>>(a);
     ++g_launches;
     return cudaGetLastError();
 }
@@ -274,13 +298,50 @@ __global__ void __launch_bounds__(256, 3) splat_kernel(RaySoA q, const int64_t* 
     add_stats(st, 0, done);
 }
 
+// The same splat through the block's shared texel table: the block takes
+// 256 queued rays at a time and, plane by plane, sums their samples per
+// texel before one map atomic per distinct texel.
+__global__ void __launch_bounds__(256, 3) splat_agg_kernel(RaySoA q, const int64_t* __restrict__ d_count,
+                                                           const splat_ftri_t* __restrict__ tris, SplatParams sp,
+                                                           splat_trace_stats_t* st) {
+    __shared__ int32_t s_key[kAggSlots], s_val[kAggSlots];
+    const int64_t n = *d_count;
+    const int planes = sp.n_lambda > 0 ? sp.n_lambda : 1;
+    const TableSink sink{sp, s_key, s_val};
+    table_clear(s_key, s_val);
+    __syncthreads();
+    int done = 0;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = base + threadIdx.x;
+        const bool live = k < n;
+        RayState r;
+        Tri T;
+        TriUV quv;
+        if (live) {
+            r = load_ray(q, k);
+            T = load_tri(tris, r.ignore);
+            quv = tri_uv(T);
+        }
+        for (int il = 0; il < planes; ++il) {
+            if (live) done += splat_ray_plane(sp, r, T, quv, il, sink);
+            __syncthreads();
+            table_flush(sp, s_key, s_val);
+            __syncthreads();
+        }
+    }
+    add_stats(st, 0, done);
+}
+
 cudaError_t launch_splat(const RaySoA& q, const int64_t* d_count, const splat_ftri_t* tris, const SplatParams& sp,
                          splat_trace_stats_t* stats, int sm_count, cudaStream_t s) {
     if (q.cap <= 0) return cudaSuccess;
     int64_t b = (q.cap + 255) / 256;
     const int64_t lim = (int64_t)sm_count * g_tune[SPLAT_TUNE_SPLAT_BLOCKS_PER_SM];
     if (b > lim) b = lim;
-    splat_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_count, tris, sp, stats);
+    if (g_tune[SPLAT_TUNE_SPLAT_AGGREGATE])
+        splat_agg_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_count, tris, sp, stats);
+    else
+        splat_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_count, tris, sp, stats);
     ++g_launches;
     return cudaGetLastError();
 }

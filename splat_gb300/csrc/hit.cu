@@ -23,7 +23,7 @@
 namespace splat {
 
 thread_local int64_t g_launches = 0;
-int32_t g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8};
+int32_t g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0};
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + bulk copy (sm_90+ async proxy)

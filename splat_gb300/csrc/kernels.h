@@ -10,7 +10,7 @@ namespace splat {
 
 // Kernels launched by this thread (for launch profiling).
 extern thread_local int64_t g_launches;
-// Launch-shape knobs, indexed by SPLAT_TUNE_* (blocks per SM).
+// Launch-shape knobs, indexed by SPLAT_TUNE_*.
 extern int32_t g_tune[SPLAT_TUNE_KEYS];
 
 // Where a hit kernel reads its rays: the structure-of-arrays bounce state
@@ -129,11 +129,49 @@ struct EvolveArgs {
     splat_adray_t* aos;     // plugin mode: retired rays written back here
     RaySoA splat_q;         // trace mode: final-evolved diffuse rays (ignore = hit triangle)
     int64_t* splat_count;
+    RaySoA sky_q;           // camera mode: rays that escaped, unchanged
+    int64_t* sky_count;
 };
 cudaError_t launch_evolve_trace(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s);
+// trace mode plus the escaped rays queued for the skydome (camera pass)
+cudaError_t launch_evolve_camera(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s);
 cudaError_t launch_evolve_plugin(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s);
 cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_idx, const splat_ftri_t* tris,
                              int64_t n_tris, int32_t* err, const SplatParams& sp, int sm_count, cudaStream_t s);
+// camera pass (shade.cu)
+struct CameraParams {
+    splat_camera_t cam;
+    int64_t h, w;      // camera grid (image / upscale)
+    uint64_t seed;
+    float lambda;
+    double cos45;      // 1 / sqrt(2), the reference's _COS_45 (src/geo.jl:13)
+};
+struct ShadeParams {
+    cudaTextureObject_t map_tex, sky_tex;
+    int64_t map_w, map_h, sky_w, sky_h;
+    int32_t has_sky;
+    int32_t n_lambda;
+    int32_t nd;          // upscale: nd x nd sub-samples (pixels) per camera ray
+    int64_t cam_h;       // camera grid rows
+    int64_t height;      // image rows
+    float* rgb;          // image, column-major RGB float triples
+    float deltas[16];    // upres(nd)
+    float spectrum[SPLAT_MAX_LAMBDA];
+    float retina[3][SPLAT_MAX_LAMBDA];
+};
+cudaError_t launch_camera_soa(const CameraParams& c, int64_t n, RaySoA out, int64_t* count, int sm_count,
+                              cudaStream_t s);
+cudaError_t launch_camera_aos(const CameraParams& c, int64_t n, splat_adray_t* out, int sm_count, cudaStream_t s);
+cudaError_t launch_shade_queues(const RaySoA& dq, const int64_t* d_count, const RaySoA& sq, const int64_t* s_count,
+                                const splat_ftri_t* tris, const ShadeParams& p, int64_t cap, int sm_count,
+                                cudaStream_t s);
+cudaError_t launch_shade_aos(splat_adray_t* rays, int64_t n, const int32_t* hit_idx, const splat_ftri_t* tris,
+                             int64_t n_tris, int32_t* err, const ShadeParams& p, int sm_count, cudaStream_t s);
+cudaError_t launch_image_accumulate(float* out, const float* rgb, int64_t n, int32_t k, int sm_count,
+                                    cudaStream_t s);
+cudaError_t launch_map_to_array(const int32_t* map, int64_t w, int64_t h, int64_t planes, float inv_scale,
+                                cudaSurfaceObject_t surf, int sm_count, cudaStream_t s);
+
 // light-map splat of the queued diffuse rays, one thread per (ray, sample)
 cudaError_t launch_splat(const RaySoA& q, const int64_t* d_count, const splat_ftri_t* tris, const SplatParams& sp,
                          splat_trace_stats_t* stats, int sm_count, cudaStream_t s);

@@ -264,10 +264,10 @@ struct EvolveView {
     bool last;  // trace mode: the last bounce, survivors are dropped
 };
 
-constexpr int kFateDrop = 0;      // miss in trace mode, or a survivor of the last bounce
+constexpr int kFateDrop = 0;      // trace mode: a survivor of the last bounce
 constexpr int kFateKeep = 1;      // evolved, active in the next bounce (o)
 constexpr int kFateDiffuse = 2;   // hit a diffuse triangle (trace mode: o is final-evolved)
-constexpr int kFateInfinity = 3;  // plugin mode: missed everything
+constexpr int kFateInfinity = 3;  // missed everything; the ray is unchanged
 
 __device__ __forceinline__ void final_evolution(const RayState& r, const HitDerivs& h, int32_t i, RayState& o);
 
@@ -288,7 +288,7 @@ __device__ __forceinline__ int evolve_one(const RayState& r, int32_t i, uint32_t
         if (TRACE) final_evolution(r, h, ih, o);
         return kFateDiffuse;
     }
-    if (isinf(h.t)) return TRACE ? kFateDrop : kFateInfinity;
+    if (isinf(h.t)) return kFateInfinity;
     if (TRACE && v.last) return kFateDrop;
     const float u = v.force_rand >= 0.0f ? v.force_rand : fresnel_draw(v.seed, rng_id, v.bounce);
     handle_optics(r, h, ih, T, v.material, u, v.quirks, o);
@@ -416,10 +416,116 @@ __device__ __forceinline__ void flush_texel(const SplatParams& sp, int32_t off, 
         atomicAdd(reinterpret_cast<float*>(sp.map) + off, vf);
 }
 
+// Sends a texel's partial sum straight to the map.
+struct DirectSink {
+    const SplatParams& sp;
+    __device__ __forceinline__ void operator()(int32_t off, int32_t vi, float vf) const { flush_texel(sp, off, vi, vf); }
+};
+
+// Block-level texel aggregation.  Samples of the rays a block holds are
+// summed per texel in a shared open-addressing table (texel offset -> partial
+// sum) and the table is flushed with one map atomic per distinct texel.  Rays
+// that are neighbours in the queue land on neighbouring texels, so this folds
+// many map atomics (and the L2 serialisation on hot caustic texels) into
+// shared-memory ones.  int32 sums wrap exactly like the map's own atomics, so
+// fixed-point maps are bit-identical to direct accumulation; float maps
+// differ by summation order only.  A sample that finds no slot within
+// kAggProbes goes straight to the map.
+constexpr int kAggLog2 = 11;
+constexpr int kAggSlots = 1 << kAggLog2;
+constexpr int kAggProbes = 16;
+
+struct TableSink {
+    const SplatParams& sp;
+    int32_t* keys;  // shared, -1 = empty
+    int32_t* vals;  // shared, int32 sum or float bits
+    __device__ __forceinline__ void operator()(int32_t off, int32_t vi, float vf) const {
+        if (off < 0) return;
+        uint32_t h = ((uint32_t)off * 2654435761u) >> (32 - kAggLog2);
+        for (int p = 0; p < kAggProbes; ++p) {
+            const int32_t k = atomicCAS(&keys[h], -1, off);
+            if (k == -1 || k == off) {
+                if (sp.accum == SPLAT_ACCUM_I32) atomicAdd(&vals[h], vi);
+                else atomicAdd(reinterpret_cast<float*>(&vals[h]), vf);
+                return;
+            }
+            h = (h + 1) & (kAggSlots - 1);
+        }
+        flush_texel(sp, off, vi, vf);
+    }
+};
+
+// The table of a block whose rays splat into different maps (the batch
+// engine): keyed by the texel's address, its low bit set for float maps.
+struct AddrTableSink {
+    const SplatParams& sp;
+    unsigned long long* keys;  // shared, 0 = empty
+    int32_t* vals;
+    __device__ __forceinline__ void operator()(int32_t off, int32_t vi, float vf) const {
+        if (off < 0) return;
+        const bool f32 = sp.accum != SPLAT_ACCUM_I32;
+        const unsigned long long key =
+            (unsigned long long)(reinterpret_cast<uintptr_t>(sp.map) + 4ull * (uint32_t)off) | (f32 ? 1ull : 0ull);
+        uint32_t h = (uint32_t)(((key >> 2) * 0x9E3779B97F4A7C15ull) >> (64 - kAggLog2));
+        for (int p = 0; p < kAggProbes; ++p) {
+            const unsigned long long k = atomicCAS(&keys[h], 0ull, key);
+            if (k == 0ull || k == key) {
+                if (!f32) atomicAdd(&vals[h], vi);
+                else atomicAdd(reinterpret_cast<float*>(&vals[h]), vf);
+                return;
+            }
+            h = (h + 1) & (kAggSlots - 1);
+        }
+        flush_texel(sp, off, vi, vf);
+    }
+};
+
+__device__ __forceinline__ void addr_table_clear(unsigned long long* keys, int32_t* vals) {
+    for (int i = threadIdx.x; i < kAggSlots; i += blockDim.x) {
+        keys[i] = 0ull;
+        vals[i] = 0;
+    }
+}
+
+__device__ __forceinline__ void addr_table_flush(unsigned long long* keys, int32_t* vals) {
+    for (int i = threadIdx.x; i < kAggSlots; i += blockDim.x) {
+        const unsigned long long k = keys[i];
+        if (k != 0ull) {
+            const int32_t v = vals[i];
+            if (k & 1ull) atomicAdd(reinterpret_cast<float*>(k & ~3ull), __int_as_float(v));
+            else atomicAdd(reinterpret_cast<int*>(k), v);
+            keys[i] = 0ull;
+            vals[i] = 0;
+        }
+    }
+}
+
+__device__ __forceinline__ void table_clear(int32_t* keys, int32_t* vals) {
+    for (int i = threadIdx.x; i < kAggSlots; i += blockDim.x) {
+        keys[i] = -1;
+        vals[i] = 0;
+    }
+}
+
+// Every thread of the block calls this between two __syncthreads().
+__device__ __forceinline__ void table_flush(const SplatParams& sp, int32_t* keys, int32_t* vals) {
+    for (int i = threadIdx.x; i < kAggSlots; i += blockDim.x) {
+        const int32_t k = keys[i];
+        if (k >= 0) {
+            const int32_t v = vals[i];
+            flush_texel(sp, k, v, __int_as_float(v));
+            keys[i] = -1;
+            vals[i] = 0;
+        }
+    }
+}
+
 // The N x N sub-samples of one (ray, plane), x offset fastest; returns the
-// number of samples accumulated.
+// number of samples accumulated.  Consecutive samples on one texel are summed
+// in registers before they reach the sink.
+template <class Sink>
 __device__ __forceinline__ int splat_ray_plane(const SplatParams& sp, const RayState& r, const Tri& T,
-                                               const TriUV& quv, int il) {
+                                               const TriUV& quv, int il, const Sink& sink) {
     const int nd = sp.n_delta;
     const int32_t W = (int32_t)sp.w, H = (int32_t)sp.h;
     const float Wf = (float)W, Hf = (float)H;
@@ -454,15 +560,20 @@ __device__ __forceinline__ int splat_ray_plane(const SplatParams& sp, const RayS
                 run_i += vi;
                 run_f += inten;
             } else {
-                flush_texel(sp, run_off, run_i, run_f);
+                sink(run_off, run_i, run_f);
                 run_off = off;
                 run_i = vi;
                 run_f = inten;
             }
         }
     }
-    flush_texel(sp, run_off, run_i, run_f);
+    sink(run_off, run_i, run_f);
     return done;
+}
+
+__device__ __forceinline__ int splat_ray_plane(const SplatParams& sp, const RayState& r, const Tri& T,
+                                               const TriUV& quv, int il) {
+    return splat_ray_plane(sp, r, T, quv, il, DirectSink{sp});
 }
 
 }  // namespace splat

@@ -405,3 +405,37 @@ def served_request(rng, scene, first_diffuse: int, rid: int) -> Workload:
                     lambda_mode=(T.LAMBDA_STRATIFIED, planes, 400.0, 700.0), spectrum=stratified_spectrum(planes),
                     depth=depth, material=CAUCHY_GLASS, map_w=side, map_h=side, accum="i32", hitter="bvh",
                     seed=1000003 + rid)
+
+
+# -------------------------------------------------------------------------- camera pass
+def realtime_camera() -> dict:
+    """A view of the realtime scene (sphere at the origin over the floor at
+    y = -1.5), 45-degree field of view (src/scenes/sphere.jl:55-62 style)."""
+    return {"pos": (0.0, 2.5, 5.0), "look_at": (0.0, -0.5, 0.0), "up": (0.0, 1.0, 0.0), "fov": 45.0 * np.pi / 180.0}
+
+
+def gradient_sky(w: int = 512, h: int = 256, seed: int = 6) -> np.ndarray:
+    """Procedural skydome [w, h, 3] float32 in [0, 1] (the reference loads
+    objs/skydome2.png, which it does not ship): a vertical gradient with seeded
+    value-noise clouds."""
+    u = (np.arange(w, dtype=np.float64) + 0.5) / w  # polar angle / pi
+    v = (np.arange(h, dtype=np.float64) + 0.5) / h  # azimuth
+    U, Vv = np.meshgrid(u, v, indexing="ij")
+    pts = np.stack([U * 8.0, Vv * 16.0, np.zeros_like(U)], axis=-1).reshape(-1, 3)
+    cloud = value_noise(pts, 1.0, seed).reshape(w, h)
+    sky = np.zeros((w, h, 3), dtype=np.float32, order="F")
+    sky[:, :, 0] = 0.25 + 0.5 * U + 0.2 * cloud
+    sky[:, :, 1] = 0.45 + 0.35 * U + 0.2 * cloud
+    sky[:, :, 2] = 0.9 - 0.3 * U + 0.1 * cloud
+    return np.clip(sky, 0.0, 1.0)
+
+
+def checkered_map(pixels_per_square: int, squares: int, planes: int, value: float = 12.0) -> np.ndarray:
+    """checkered_tex(pixels_per_square, squares, planes) .* value
+    (src/procedural_assets.jl:86-97, src/scenes/sphere.jl:43): [w, h, planes]
+    float32, w = h = 2 pixels_per_square squares."""
+    x = np.tile(np.concatenate([np.ones(pixels_per_square), np.zeros(pixels_per_square)]), squares)
+    t = (x[:, None] + x[None, :]) % 2
+    out = np.zeros((len(x), len(x), planes), dtype=np.float32, order="F")
+    out[:, :, :] = (t * value)[:, :, None]
+    return out

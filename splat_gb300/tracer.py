@@ -312,3 +312,210 @@ def trace_forward(wl, scene: Optional[Scene] = None, ray_begin: int = 0, ray_end
     tex = step.run()
     _torch().cuda.synchronize()
     return StepResult(tex, step.stats())
+
+
+# ---------------------------------------------------------------------------
+# camera pass: the backward half of trace! (src/tracer.jl:345-378)
+# ---------------------------------------------------------------------------
+def camera_look_at(pos, look_at, up, fov: float) -> L.Camera:
+    """get_camera (src/geo.jl:183-191); fov in radians."""
+    cam = L.Camera()
+    f = lambda v: (C.c_float * 3)(*[float(x) for x in v])  # noqa: E731
+    L.check(L.load().splat_camera_look_at(f(pos), f(look_at), f(up), float(fov), C.byref(cam)))
+    return cam
+
+
+def camera_rays(cam: L.Camera, height: int, width: int, lam: float = 550.0, seed: int = 0):
+    """wrap_ray_gen(camera_ray) (src/ray_generators.jl:18-62) over a
+    height x width grid: a device ADRay buffer in pixel order."""
+    torch = _torch()
+    out = torch.empty(int(height) * int(width) * T.ADRAY.itemsize, dtype=torch.uint8, device="cuda")
+    L.check(L.load().splat_camera_rays(C.byref(cam), int(height), int(width), float(lam), int(seed), _ptr(out),
+                                       _stream()))
+    return out
+
+
+def retina_factors(spectrum) -> np.ndarray:
+    """_spectrum_datastructs (src/rgb_spectrum.jl:135-149): [3, n] float32."""
+    spec = np.ascontiguousarray(spectrum, dtype=np.float32)
+    out = np.zeros((3, len(spec)), dtype=np.float32)
+    L.check(L.load().splat_retina_factors(spec.ctypes.data, len(spec), out.ctypes.data))
+    return out
+
+
+def new_image(height: int, width: int):
+    """RGB image, column-major pixels (the reference's RGBf array): a
+    (width, height, 3) float32 tensor; image(t) gives [row, col, channel]."""
+    return _torch().zeros((int(width), int(height), 3), dtype=_torch().float32, device="cuda")
+
+
+def image(rgb) -> np.ndarray:
+    return rgb.cpu().numpy().transpose(1, 0, 2)
+
+
+class Shader:
+    """The light map and skydome as linear-filtered 3-D textures (the
+    reference's CuTexture objects), device arrays reused across frames."""
+
+    def __init__(self, map_w: int, map_h: int, planes: int, sky_w: int = 0, sky_h: int = 0):
+        h = C.c_void_p()
+        L.check(L.load().splat_shader_create(int(map_w), int(map_h), int(planes), int(sky_w), int(sky_h), C.byref(h)))
+        self._h = h
+        self.map_w, self.map_h, self.planes = int(map_w), int(map_h), int(planes)
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise L.SplatError(L.ERR_INVALID, "shader is closed")
+        return self._h
+
+    def set_light_map(self, tex, frac_bits: int = 16) -> None:
+        """tex: a light map tensor (planes, h, w) from new_light_map."""
+        torch = _torch()
+        accum = L.ACCUM_F32 if tex.dtype == torch.float32 else L.ACCUM_I32
+        assert tuple(tex.shape) == (self.planes, self.map_h, self.map_w)
+        L.check(L.load().splat_shader_set_light_map(self.handle, _ptr(tex), accum, int(frac_bits), _stream()))
+
+    def set_skydome(self, sky) -> None:
+        """sky: float32 tensor (3, sky_h, sky_w) = the reference's [w, h, 3]."""
+        L.check(L.load().splat_shader_set_skydome(self.handle, _ptr(sky.contiguous()), _stream()))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None:
+            L.load().splat_shader_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def continuum_shade(scene: Scene, shader: Shader, d_rays, hit_idx, spectrum, retina, upscale: int, height: int,
+                    width: int, rgb=None):
+    """continuum_shade!(ExperimentalImager2) (src/ray_imagers.jl:441-503) on
+    rays after run_evolution: returns the (width, height, 3) image tensor."""
+    spec = np.ascontiguousarray(spectrum, dtype=np.float32)
+    ret = np.ascontiguousarray(retina, dtype=np.float32).reshape(3, len(spec))
+    if rgb is None:
+        rgb = new_image(height, width)
+    L.check(L.load().splat_continuum_shade(scene.handle, shader.handle, _ptr(d_rays), n_rays_of(d_rays),
+                                           _ptr(hit_idx), spec.ctypes.data, ret.ctypes.data, len(spec),
+                                           int(upscale), int(height), int(width), _ptr(rgb), _stream()))
+    return rgb
+
+
+def render_params(cam: L.Camera, height: int, width: int, upscale: int, depth: int, material, spectrum,
+                  hitter: str = "bvh", seed: int = 0, force_rand: Optional[float] = None, quirks: bool = True,
+                  lam: float = 550.0) -> L.RenderParams:
+    P = L.RenderParams()
+    P.camera = cam
+    P.height, P.width, P.upscale = int(height), int(width), int(upscale)
+    P.seed = int(seed)
+    P.depth = int(depth)
+    P.hitter = {"bvh": BVH, "bvh2": BVH2, "brute": BRUTE}[hitter]
+    P.material = _material(material)
+    P.force_rand = -1.0 if force_rand is None else float(force_rand)
+    P.flags = L.FLAG_REF_QUIRKS if quirks else 0
+    P.lambda_ = float(lam)
+    spec = np.asarray(spectrum, dtype=np.float32)
+    ret = retina_factors(spec)
+    P.n_lambda = len(spec)
+    for i, v in enumerate(spec):
+        P.spectrum[i] = float(v)
+        for c in range(3):
+            P.retina[c][i] = float(ret[c, i])
+    return P
+
+
+class CameraPass:
+    """The fused camera pass (splat_render_camera) with its workspace and
+    image resident."""
+
+    def __init__(self, scene: Scene, shader: Shader, params: L.RenderParams):
+        torch = _torch()
+        self.scene, self.shader, self.params = scene, shader, params
+        n = (params.height // params.upscale) * (params.width // params.upscale)
+        self.ws = torch.empty(int(L.load().splat_render_workspace_size(n)), dtype=torch.uint8, device="cuda")
+        self.rgb = new_image(params.height, params.width)
+
+    def run(self, stream: Optional[int] = None):
+        L.check(L.load().splat_render_camera(self.scene.handle, self.shader.handle, C.byref(self.params),
+                                             _ptr(self.rgb), _ptr(self.ws), self.ws.numel(),
+                                             _stream() if stream is None else stream))
+        return self.rgb
+
+
+_GOLDEN = 0x9E3779B97F4A7C15
+_ITER = 0xBF58476D1CE4E5B9
+_CAMERA_SALT = 0xD1B54A32D192ED03
+_M64 = (1 << 64) - 1
+
+
+def forward_seed(seed: int, light: int, iteration: int) -> int:
+    """Philox key of light `light` (0-based) in iteration `iteration` (1-based)
+    of a frame: the workload's own seed for light 0 of iteration 1."""
+    return (int(seed) + light * _GOLDEN + (iteration - 1) * _ITER) & _M64
+
+
+def camera_seed(seed: int, iteration: int) -> int:
+    return ((int(seed) ^ _CAMERA_SALT) + (iteration - 1) * _ITER) & _M64
+
+
+class Renderer:
+    """trace! (src/tracer.jl:287-388): per iteration, the forward step of every
+    light into the light map (onto a base map, the reference's tex_f()), the
+    map into the shader's texture, the camera pass, and the running average of
+    the iterations' images.  Light i of iteration k draws with
+    forward_seed(seed, i, k); the camera pass with camera_seed(seed, k)."""
+
+    def __init__(self, wl, cam: L.Camera, height: int, width: int, upscale: int = 2, lights: Optional[Sequence] = None,
+                 sky=None, base_map=None, iterations: int = 1, scene: Optional[Scene] = None,
+                 camera_depth: Optional[int] = None, camera_hitter: Optional[str] = None):
+        torch = _torch()
+        if wl.spectrum is None:
+            raise ValueError("rendering needs a spectrum (one light-map plane per wavelength)")
+        self.wl = wl
+        self.step = TraceStep(wl, scene)
+        self.scene = self.step.scene
+        self.lights = list(lights) if lights is not None else [wl.light]
+        n_max = max(int(li["res1"] // wl.upscale) * int(li["res2"] // wl.upscale) for li in self.lights)
+        if n_max > self.step.n:
+            self.step.ws = torch.empty(int(L.load().splat_trace_workspace_size(n_max)), dtype=torch.uint8,
+                                       device="cuda")
+            self.step.n = n_max
+        self.iterations = int(iterations)
+        sw, sh = (0, 0) if sky is None else (int(sky.shape[2]), int(sky.shape[1]))
+        self.shader = Shader(wl.map_w, wl.map_h, wl.n_planes, sw, sh)
+        if sky is not None:
+            self.shader.set_skydome(sky)
+        self.base = base_map
+        self.params = render_params(cam, height, width, upscale, camera_depth or wl.depth, wl.material, wl.spectrum,
+                                    camera_hitter or wl.hitter, camera_seed(wl.seed, 1), wl.force_rand, wl.quirks)
+        self.camera = CameraPass(self.scene, self.shader, self.params)
+        self.out = new_image(height, width)
+        self.n_values = self.out.numel()
+        self._torch = torch
+
+    def forward(self, iteration: int = 1):
+        P = self.step.params
+        for i, light in enumerate(self.lights):
+            P.light = _light(light)
+            P.seed = forward_seed(self.wl.seed, i, iteration)
+            first = i == 0
+            if first and self.base is not None:
+                self.step.tex.copy_(self.base)
+            P.zero_map = 1 if first and self.base is None else 0
+            self.step.run()
+        return self.step.tex
+
+    def run(self):
+        lib = L.load()
+        for k in range(1, self.iterations + 1):
+            self.forward(k)
+            self.shader.set_light_map(self.step.tex, self.wl.frac_bits)
+            self.params.seed = camera_seed(self.wl.seed, k)
+            rgb = self.camera.run()
+            L.check(lib.splat_image_accumulate(_ptr(self.out), _ptr(rgb), self.n_values, k, _stream()))
+        return self.out

@@ -47,6 +47,10 @@ int main(void) {
   O(splat_trace_params_t, force_rand) O(splat_trace_params_t, spectrum) O(splat_trace_params_t, map_w)
   O(splat_trace_params_t, accum) O(splat_trace_params_t, ray_begin) O(splat_trace_params_t, ray_end)
   O(splat_scene_info_t, device_bytes) O(splat_scene_info_t, bvh_pad)
+  P(splat_camera_t) P(splat_render_params_t)
+  O(splat_camera_t, right) O(splat_camera_t, fov_half_sin)
+  O(splat_render_params_t, height) O(splat_render_params_t, seed) O(splat_render_params_t, material)
+  O(splat_render_params_t, lambda) O(splat_render_params_t, spectrum) O(splat_render_params_t, retina)
   return 0;
 }
 """
@@ -80,6 +84,13 @@ def test_record_layouts_match_header():
     assert c["splat_scene_info_t.bvh_pad"] == L.SceneInfo.bvh_pad.offset
     for f, off in [("in_medium", 96), ("ignore_tri", 104), ("dest", 112), ("lam", 120), ("status", 132)]:
         assert T.ADRAY.fields[f][1] == off
+    # Cam (src/geo.jl:50-57): five R3 and a Float32
+    assert c["splat_camera_t"] == 64 == C.sizeof(L.Camera)
+    assert c["splat_camera_t.right"] == 48 and c["splat_camera_t.fov_half_sin"] == 60
+    assert c["splat_render_params_t"] == C.sizeof(L.RenderParams)
+    for f in ["height", "seed", "material", "spectrum", "retina"]:
+        assert c[f"splat_render_params_t.{f}"] == getattr(L.RenderParams, f).offset, f
+    assert c["splat_render_params_t.lambda"] == L.RenderParams.lambda_.offset
 
 
 def test_invalid_arguments_fail_cleanly_without_gpu():
@@ -94,3 +105,24 @@ def test_invalid_arguments_fail_cleanly_without_gpu():
     assert lib.splat_trace_workspace_size(1000) > 1000 * 117 * 2
     with pytest.raises(L.SplatError):
         L.check(L.ERR_INVALID)
+
+
+def test_tuning_knobs_validate_and_round_trip_without_gpu():
+    """splat_set_tuning / splat_get_tuning are host-only: ranges are checked
+    and values read back; unknown keys fail."""
+    lib = L.load()
+    old = {k: lib.splat_get_tuning(k) for k in range(5)}
+    try:
+        assert old[L.TUNE_SPLAT_AGGREGATE] in (0, 1)
+        assert lib.splat_set_tuning(L.TUNE_SPLAT_AGGREGATE, 2) == L.ERR_INVALID
+        assert lib.splat_set_tuning(L.TUNE_SPLAT_AGGREGATE, 0) == L.OK
+        assert lib.splat_get_tuning(L.TUNE_SPLAT_AGGREGATE) == 0
+        assert lib.splat_set_tuning(L.TUNE_BVH_BLOCKS_PER_SM, 0) == L.ERR_INVALID
+        assert lib.splat_set_tuning(L.TUNE_BVH_BLOCKS_PER_SM, 257) == L.ERR_INVALID
+        assert lib.splat_set_tuning(L.TUNE_BVH_BLOCKS_PER_SM, 12) == L.OK
+        assert lib.splat_get_tuning(L.TUNE_BVH_BLOCKS_PER_SM) == 12
+        assert lib.splat_set_tuning(5, 1) == L.ERR_INVALID
+        assert lib.splat_get_tuning(5) == -1 and lib.splat_get_tuning(-1) == -1
+    finally:
+        for k, v in old.items():
+            L.check(lib.splat_set_tuning(k, v))

@@ -124,3 +124,40 @@ def test_host_entry_point_matches_device(torch_cuda):
     st = step.run_host(np.ascontiguousarray(wl.tris), host_map)
     assert np.array_equal(host_map, dev)
     assert st["rays_per_bounce"] == step.stats()["rays_per_bounce"]
+
+
+@pytest.mark.parametrize("accum", ["i32", "f32"])
+def test_splat_aggregation_matches_direct_atomics(torch_cuda, accum):
+    """The splat's shared-memory texel table (tuning knob) against direct map
+    atomics: int32 maps bit-identical, float maps within 1e-5 relative L1;
+    the reduced workload also against the oracle."""
+    from splat_gb300 import _lib as L
+    from splat_gb300 import tracer
+
+    lib = L.load()
+    old = lib.splat_get_tuning(L.TUNE_SPLAT_AGGREGATE)
+    wl = S.realtime(light=S.scaled_light(S.realtime().light, 384), accum=accum)
+    scene = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
+    try:
+        L.check(lib.splat_set_tuning(L.TUNE_SPLAT_AGGREGATE, 1))
+        agg, sa = _gpu(wl, scene=scene)
+        L.check(lib.splat_set_tuning(L.TUNE_SPLAT_AGGREGATE, 0))
+        direct, sd = _gpu(wl, scene=scene)
+    finally:
+        L.check(lib.splat_set_tuning(L.TUNE_SPLAT_AGGREGATE, old))
+    assert sa == sd and agg.sum() > 0
+    if accum == "i32":
+        assert np.array_equal(agg, direct)
+    else:
+        assert rel_l1(agg, direct) <= 1e-5
+    n = wl.n_rays
+    h = int(wl.light["res1"]) // wl.upscale
+    lo = n // 2 + h // 2 - 500
+    L.check(lib.splat_set_tuning(L.TUNE_SPLAT_AGGREGATE, 1))
+    try:
+        got, st = _gpu(wl, lo, lo + 1000, scene=scene)
+    finally:
+        L.check(lib.splat_set_tuning(L.TUNE_SPLAT_AGGREGATE, old))
+    ref_tex, ref_st, _ = O.trace_forward(wl, lo, lo + 1000)
+    assert st["rays_per_bounce"] == [int(x) for x in ref_st[: wl.depth]]
+    _cmp(wl, got, ref_tex)
