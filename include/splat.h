@@ -188,6 +188,13 @@ splat_status_t splat_scene_update(splat_scene_t* scene, const splat_ftri_t* d_tr
 /* Device pointer of the scene's FTri array (read-only). */
 const splat_ftri_t* splat_scene_tris(const splat_scene_t* scene);
 
+/* Mesh ingest: a Wavefront OBJ file -> FTri records (mesh_to_FTri over the
+ * faces MeshIO loads, src/geo.jl:289-341): one record per triangle, polygons
+ * fan-triangulated, per-corner positions / normals / uvs, plane normal
+ * cross(v1 - v2, v2 - v3).  No sentinel is prepended (the scene does that).
+ * Call with out = NULL to get the count, then with capacity >= count. */
+splat_status_t splat_obj_to_ftri(const char* path, splat_ftri_t* out, int64_t capacity, int64_t* n_tris);
+
 /* -------------------------------------------------------- plugin boundary */
 /* rays_from_light (src/ray_generators.jl:64-97): (res1/upscale)*(res2/upscale)
  * rays, column-major over (row, col), jitter from Philox(seed). */

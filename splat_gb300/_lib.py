@@ -108,6 +108,7 @@ SIGNATURES = {
     "splat_trace_workspace_size": ([i64], sz),
     "splat_trace_forward": ([vp, C.POINTER(TraceParams), vp, vp, sz, vp, vp], i32),
     "splat_trace_forward_host": ([vp, vp, C.POINTER(TraceParams), vp, vp, vp, sz, C.POINTER(TraceStats), vp], i32),
+    "splat_obj_to_ftri": ([C.c_char_p, vp, i64, C.POINTER(C.c_int64)], i32),
     "splat_camera_look_at": ([vp, vp, vp, C.c_double, C.POINTER(Camera)], i32),
     "splat_camera_rays": ([C.POINTER(Camera), i64, i64, f32, u64, vp, vp], i32),
     "splat_retina_factors": ([vp, i32, vp], i32),

@@ -9,6 +9,7 @@
 
 #include "bvh_build.h"
 #include "kernels.h"
+#include "mesh.h"
 
 using namespace splat;
 
@@ -1512,5 +1513,17 @@ splat_status_t splat_image_accumulate(float* d_out, const float* d_rgb, int64_t 
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     ProfScope ps(SPLAT_KERNEL_SHADE, st);
     SPLAT_CUDA(launch_image_accumulate(d_out, d_rgb, n, iteration, sm_count_current(), st), "image_accumulate");
+    return SPLAT_OK;
+}
+
+splat_status_t splat_obj_to_ftri(const char* path, splat_ftri_t* out, int64_t capacity, int64_t* n_tris) {
+    if (!path || !n_tris) return fail(SPLAT_ERR_INVALID, "obj_to_ftri: null argument");
+    std::vector<splat_ftri_t> tris;
+    std::string err;
+    if (!obj_to_ftri(path, tris, err)) return fail(SPLAT_ERR_INVALID, "obj_to_ftri: " + err);
+    *n_tris = (int64_t)tris.size();
+    if (!out) return SPLAT_OK;
+    if (capacity < (int64_t)tris.size()) return fail(SPLAT_ERR_WORKSPACE, "obj_to_ftri: capacity below the count");
+    std::memcpy(out, tris.data(), tris.size() * sizeof(splat_ftri_t));
     return SPLAT_OK;
 }

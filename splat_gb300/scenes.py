@@ -26,7 +26,7 @@ reference's scenes arrange them (src/scenes/sphere.jl:36-37).
 from __future__ import annotations
 
 from dataclasses import dataclass, field, replace
-from typing import Optional
+from typing import Sequence, Optional
 
 import numpy as np
 
@@ -438,4 +438,54 @@ def checkered_map(pixels_per_square: int, squares: int, planes: int, value: floa
     t = (x[:, None] + x[None, :]) % 2
     out = np.zeros((len(x), len(x), planes), dtype=np.float32, order="F")
     out[:, :, :] = (t * value)[:, :, None]
+    return out
+
+
+# -------------------------------------------------------------------------- mesh ingest
+def load_obj(path: str) -> np.ndarray:
+    """A Wavefront OBJ file as FTri records (T, 10, 3) through libsplat's
+    parser (mesh_to_FTri, src/geo.jl:330-341); no sentinel."""
+    import ctypes as C
+
+    from . import _lib as L
+
+    lib = L.load()
+    n = C.c_int64()
+    L.check(lib.splat_obj_to_ftri(path.encode(), None, 0, C.byref(n)))
+    out = np.zeros((n.value, 10, 3), dtype=np.float32)
+    L.check(lib.splat_obj_to_ftri(path.encode(), out.ctypes.data, n.value, C.byref(n)))
+    return out
+
+
+def write_obj(path: str, P: np.ndarray, N: np.ndarray, UV: np.ndarray) -> None:
+    """Per-corner positions / normals / uvs (T, 3, 3) as an OBJ file with
+    shortest round-trip binary32 decimals (one v / vn / vt per corner)."""
+    def f(x):
+        return repr(float(np.float32(x)))
+
+    with open(path, "w") as fh:
+        fh.write("# written by splat_gb300.scenes.write_obj\n")
+        for t in range(P.shape[0]):
+            for k in range(3):
+                fh.write("v %s %s %s\n" % tuple(f(c) for c in P[t, k]))
+                fh.write("vn %s %s %s\n" % tuple(f(c) for c in N[t, k]))
+                fh.write("vt %s %s\n" % (f(UV[t, k, 0]), f(UV[t, k, 1])))
+        for t in range(P.shape[0]):
+            a = 3 * t + 1
+            fh.write(f"f {a}/{a}/{a} {a + 1}/{a + 1}/{a + 1} {a + 2}/{a + 2}/{a + 2}\n")
+
+
+def assemble_meshes(glass: Sequence[np.ndarray], diffuse: Sequence[np.ndarray]):
+    """The reference's scene layout (src/scenes/sphere.jl:36-38): the zero
+    sentinel, then the glass meshes, then the diffuse ones; returns (tris,
+    first_diffuse 1-based)."""
+    g = np.concatenate(list(glass), 0) if glass else np.zeros((0, 10, 3), np.float32)
+    d = np.concatenate(list(diffuse), 0) if diffuse else np.zeros((0, 10, 3), np.float32)
+    return assemble(g, d)
+
+
+def translate(tris: np.ndarray, offset) -> np.ndarray:
+    """translate(t::FTri, v) (src/geo.jl:132-135): vertices moved, normals and uvs kept."""
+    out = tris.copy()
+    out[:, 1:4] = (out[:, 1:4] + np.asarray(offset, np.float32)).astype(np.float32)
     return out
