@@ -185,6 +185,16 @@ splat_status_t splat_scene_info(const splat_scene_t* scene, splat_scene_info_t* 
  * geometry upload): repacks the hit records and refits the BVH boxes
  * bottom-up, keeping its topology.  d_tris: device FTri array. */
 splat_status_t splat_scene_update(splat_scene_t* scene, const splat_ftri_t* d_tris, void* stream);
+/* Device-side geometry replacement with the BVH rebuilt on the GPU: a
+ * linear BVH (Morton-ordered centroids, radix tree, bottom-up padded boxes,
+ * leaves of at most 4 triangles) in the same node formats, for scenes whose
+ * motion a refit would degrade (the reference rebuilds its bounding volumes
+ * on the host every frame, src/scenes/splash_scene.jl:41, src/bv.jl:68-121).
+ * Hits stay identical to brute force.  The first call allocates the build's
+ * scratch; later calls allocate nothing.  After a rebuild,
+ * splat_scene_update rebuilds too.  d_tris NULL: rebuild from the scene's
+ * current triangles. */
+splat_status_t splat_scene_rebuild(splat_scene_t* scene, const splat_ftri_t* d_tris, void* stream);
 /* Device pointer of the scene's FTri array (read-only). */
 const splat_ftri_t* splat_scene_tris(const splat_scene_t* scene);
 

@@ -98,6 +98,7 @@ SIGNATURES = {
     "splat_scene_info": ([vp, C.POINTER(SceneInfo)], i32),
     "splat_scene_update": ([vp, vp, vp], i32),
     "splat_scene_tris": ([vp], vp),
+    "splat_scene_rebuild": ([vp, vp, vp], i32),
     "splat_rays_from_light": ([C.POINTER(RectLight), i64, C.POINTER(LambdaMode), u64, u32, vp, vp], i32),
     "splat_next_hit_brute": ([vp, i64, vp, i64, vp, vp, vp], i32),
     "splat_next_hit_brute_static": ([vp, i64, vp, i64, vp, vp], i32),

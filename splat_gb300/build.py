@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsplat.so")
 ROOT = os.path.dirname(HERE)
 
-CU_SOURCES = ["api.cu", "hit.cu", "evolve.cu", "batch.cu", "shade.cu"]
+CU_SOURCES = ["api.cu", "hit.cu", "evolve.cu", "batch.cu", "shade.cu", "lbvh.cu"]
 CPP_SOURCES = ["bvh_build.cpp", "mesh.cpp"]
 HEADERS = ["common.cuh", "optics.cuh", "kernels.h", "bvh_build.h", "hitcore.cuh", "mesh.h"]
 

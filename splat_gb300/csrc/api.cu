@@ -76,7 +76,8 @@ struct Work {
     int64_t* counts;  // counts[b] = active rays after bounce b (b <= 64); counts[kSplatCount] = queued
 };
 constexpr int kSplatCount = 96;
-constexpr size_t kCounterBytes = 1024;
+constexpr int kFetchBase = 128;  // counts[kFetchBase + b]: work counter of bounce b's hit launch
+constexpr size_t kCounterBytes = 2048;
 
 size_t work_bytes(int64_t cap) {
     return 3 * soa_bytes(cap) + align_up(4 * (size_t)cap) + align_up(8 * (size_t)cap) + kCounterBytes + kAlign;
@@ -164,6 +165,12 @@ struct splat_scene {
     float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
     int32_t* d_err = nullptr;
     int64_t bytes = 0;
+    // GPU rebuild (linear BVH): scratch and node capacities; once the tree
+    // comes from the GPU the host level lists no longer match it, and updates
+    // rebuild instead of refitting
+    void* d_lbvh = nullptr;
+    int64_t cap_nodes = 0, cap_nodes4 = 0;
+    bool gpu_bvh = false;
 };
 
 static void scene_free(splat_scene* s) {
@@ -177,6 +184,7 @@ static void scene_free(splat_scene* s) {
     cudaFree(s->d_nodes4);
     cudaFree(s->d_levels4);
     cudaFree(s->d_err);
+    cudaFree(s->d_lbvh);
     delete s;
 }
 
@@ -273,6 +281,8 @@ splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris,
         chk(dalloc(&s->d_order, sizeof(int32_t) * bvh.order.size(), s->bytes));
         chk(dalloc(&s->d_levels, sizeof(int32_t) * bvh.level_nodes.size(), s->bytes));
         s->n_nodes4 = (int64_t)bvh.nodes4.size();
+        s->cap_nodes = s->n_nodes;
+        s->cap_nodes4 = s->n_nodes4;
         chk(dalloc(&s->d_nodes4, sizeof(Bvh4Node) * bvh.nodes4.size(), s->bytes));
         chk(dalloc(&s->d_levels4, sizeof(int32_t) * bvh.level4_nodes.size(), s->bytes));
         s->level4_off = bvh.level4_off;
@@ -338,9 +348,66 @@ splat_status_t splat_scene_info(const splat_scene_t* s, splat_scene_info_t* info
 
 const splat_ftri_t* splat_scene_tris(const splat_scene_t* s) { return s ? s->d_ftri : nullptr; }
 
+// BVH of the scene's current FTri data rebuilt on the GPU (linear BVH).
+static splat_status_t scene_rebuild_gpu(splat_scene* s, cudaStream_t st) {
+    const int64_t np = s->n_tris - 1;
+    if (np < 1) return SPLAT_OK;
+    const int64_t need = np > 1 ? np - 1 : 1;
+    auto grow = [&](auto** p, int64_t& cap, int64_t want, size_t elem) -> cudaError_t {
+        if (*p && cap >= want) return cudaSuccess;
+        cudaFree(*p);
+        *p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), elem * (size_t)want);
+        if (e == cudaSuccess) {
+            cap = want;
+            s->bytes += (int64_t)(elem * (size_t)want);
+        }
+        return e;
+    };
+    SPLAT_CUDA(grow(&s->d_nodes, s->cap_nodes, need, sizeof(BvhNode)), "scene_rebuild: node array");
+    SPLAT_CUDA(grow(&s->d_nodes4, s->cap_nodes4, need, sizeof(Bvh4Node)), "scene_rebuild: four-wide node array");
+    if (!s->d_bvh) {
+        int64_t cap = 0;
+        SPLAT_CUDA(grow(&s->d_bvh, cap, np, sizeof(TriHit)), "scene_rebuild: hit records");
+    }
+    if (!s->d_order) {
+        int64_t cap = 0;
+        SPLAT_CUDA(grow(&s->d_order, cap, np, sizeof(int32_t)), "scene_rebuild: order");
+    }
+    if (!s->d_lbvh) {
+        const size_t b = lbvh_scratch_bytes(np);
+        SPLAT_CUDA(cudaMalloc(&s->d_lbvh, b), "scene_rebuild: scratch");
+        s->bytes += (int64_t)b;
+    }
+    SPLAT_CUDA(launch_lbvh_build(s->d_ftri, s->n_tris, kLbvhLeaf, s->d_lbvh, s->d_nodes, s->d_nodes4, s->d_order,
+                                 sm_count_current(), st),
+               "scene_rebuild: build");
+    SPLAT_CUDA(launch_pack_hits(s->d_ftri, s->n_tris, s->d_brute, s->d_order, s->d_bvh, st), "scene_rebuild: pack");
+    s->gpu_bvh = true;
+    s->n_nodes = need;
+    s->n_nodes4 = need;
+    s->max_leaf = kLbvhLeaf;
+    s->depth = 0;
+    s->leaves = 0;
+    return SPLAT_OK;
+}
+
+splat_status_t splat_scene_rebuild(splat_scene_t* s, const splat_ftri_t* d_tris, void* stream) {
+    if (!s) return fail(SPLAT_ERR_INVALID, "scene_rebuild: null scene");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (d_tris && d_tris != s->d_ftri)
+        SPLAT_CUDA(cudaMemcpyAsync(s->d_ftri, d_tris, sizeof(splat_ftri_t) * (size_t)s->n_tris,
+                                   cudaMemcpyDeviceToDevice, st),
+                   "scene_rebuild copy");
+    ProfScope ps(SPLAT_KERNEL_AUX, st);
+    return scene_rebuild_gpu(s, st);
+}
+
 splat_status_t splat_scene_update(splat_scene_t* s, const splat_ftri_t* d_tris, void* stream) {
     if (!s || !d_tris) return fail(SPLAT_ERR_INVALID, "scene_update: null argument");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    if (s->gpu_bvh) return splat_scene_rebuild(s, d_tris, stream);
     if (d_tris != s->d_ftri)
         SPLAT_CUDA(cudaMemcpyAsync(s->d_ftri, d_tris, sizeof(splat_ftri_t) * (size_t)s->n_tris,
                                    cudaMemcpyDeviceToDevice, st),
@@ -511,7 +578,8 @@ splat_status_t splat_run_evolution(const splat_scene_t* scene, int32_t hitter, s
     ea.quirks = (flags & SPLAT_FLAG_REF_QUIRKS) ? 1 : 0;
     ea.aos = d_rays;
     for (int32_t b = 1; b <= depth; ++b) {
-        RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0};
+        RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0,
+                   reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b])};
         splat_status_t rc = hit_any(scene, hitter, src, n_rays, w.hit, nullptr, w.tmp, st);
         if (rc != SPLAT_OK) return rc;
         ea.in = cur;
@@ -623,7 +691,8 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
     ea.splat_count = &w.counts[kSplatCount];
     RaySoA cur = w.a, nxt = w.b;
     for (int32_t b = 1; b <= P->depth; ++b) {
-        RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0};
+        RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0,
+                   reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b])};
         rc = hit_any(scene, P->hitter, src, cnt, w.hit, nullptr, w.tmp, st);
         if (rc != SPLAT_OK) return rc;
         ea.in = cur;
@@ -858,7 +927,7 @@ splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done
     int64_t* cur_count = &b->counts[b->parity];
     int64_t* next_count = &b->counts[b->parity ^ 1];
     SPLAT_CUDA(cudaMemsetAsync(next_count, 0, sizeof(int64_t), st), "batch: reset count");
-    SPLAT_CUDA(cudaMemsetAsync(&b->counts[2], 0, sizeof(int64_t), st), "batch: reset queue");
+    SPLAT_CUDA(cudaMemsetAsync(&b->counts[2], 0, 2 * sizeof(int64_t), st), "batch: reset queue + work counter");
     if (cap_rays > 0) {
         ProfScope ps(SPLAT_KERNEL_BATCH, st);
         BatchTickArgs a;
@@ -878,6 +947,7 @@ splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done
         a.err = b->d_err;
         a.sm_count = sm_count_current();
         a.any_brute = any_brute;
+        a.fetch = reinterpret_cast<unsigned long long*>(&b->counts[3]);
         SPLAT_CUDA(launch_batch_tick(a, st), "batch tick");
         b->parity ^= 1;
     }
@@ -1482,7 +1552,8 @@ splat_status_t splat_render_camera(const splat_scene_t* scene, const splat_shade
     ea.sky_count = sky_count;
     RaySoA cur = w.a, nxt = w.b;
     for (int32_t b = 1; b <= P->depth; ++b) {
-        RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0};
+        RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0,
+                   reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b])};
         rc = hit_any(scene, P->hitter, src, cnt, w.hit, nullptr, w.tmp, st);
         if (rc != SPLAT_OK) return rc;
         ea.in = cur;

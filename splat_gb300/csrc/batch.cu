@@ -105,7 +105,7 @@ __global__ void batch_generate_kernel(const BatchItem* __restrict__ items, const
 template <bool ANY_BRUTE>
 __global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t* __restrict__ count,
                                                         const BatchItem* __restrict__ items, int32_t* hit_idx,
-                                                        int32_t* err) {
+                                                        int32_t* err, unsigned long long* fetch) {
     const int64_t n = *count;
     int stack_ref[kBvhStack];
     float stack_t[kBvhStack];
@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t
     src.f = in.f;
     src.ignore = in.ignore;
     src.cap = in.cap;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    for_each_ray(n, fetch, [&](int64_t k) {
         const HitRay r = load_hit_ray<false>(src, k);
         const BatchItem& it = items[in.id[k] >> kSlotShift];
         float best;
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t
         else
             brute_closest(r, it.brute, it.n_recs, best, bi);
         hit_idx[k] = bi;
-    }
+    });
 }
 
 constexpr int kBatchThreads = 256;
@@ -256,11 +256,14 @@ cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s) {
         ++g_launches;
     }
     if (a.cap_rays > 0) {
-        const int hg = grid_cap(a.cap_rays, 128, a.sm_count, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
         if (a.any_brute)
-            batch_hit_kernel<true><<<hg, 128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err);
+            batch_hit_kernel<true><<<resident_grid(reinterpret_cast<const void*>(batch_hit_kernel<true>), a.cap_rays,
+                                                   a.sm_count),
+                                     128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch);
         else
-            batch_hit_kernel<false><<<hg, 128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err);
+            batch_hit_kernel<false><<<resident_grid(reinterpret_cast<const void*>(batch_hit_kernel<false>), a.cap_rays,
+                                                    a.sm_count),
+                                      128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch);
         ++g_launches;
         batch_evolve_kernel<<<grid_cap(a.cap_rays, kBatchThreads, a.sm_count, 8), kBatchThreads, 0, s>>>(
             a.cur, a.next, a.queue, a.cur_count, a.next_count, a.queue_count, items, a.tick, a.hit_idx, a.err);

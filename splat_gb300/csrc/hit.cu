@@ -17,6 +17,7 @@
 //   identical to brute force.
 #include <cstdio>
 #include <mutex>
+#include <unordered_map>
 
 #include "hitcore.cuh"
 
@@ -414,13 +415,35 @@ cudaError_t launch_hit_brute_ntris_static(const splat_adray_t* rays, int64_t n_r
 // ---------------------------------------------------------------------------
 constexpr int kBvhThreads = 128;
 
+// Grid of a work-counter launch: as many 128-thread blocks as stay resident
+// together (capped by the blocks-per-SM knob and by the work), so the launch
+// is one wave that drains the counter.
+int resident_grid(const void* kernel, int64_t cap, int sm_count) {
+    static std::mutex mu;
+    static std::unordered_map<const void*, int> occ;
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = occ.find(kernel);
+        if (it == occ.end()) {
+            int nb = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kBvhThreads, 0) != cudaSuccess || nb < 1)
+                nb = 4;
+            it = occ.emplace(kernel, nb).first;
+        }
+        per_sm = it->second;
+    }
+    if (per_sm > g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]) per_sm = g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM];
+    return grid_for(cap, kBvhThreads, sm_count, per_sm);
+}
+
 template <bool AOS>
 __global__ void __launch_bounds__(kBvhThreads) hit_bvh_kernel(RaySrc src, BvhView bvh, int32_t* __restrict__ hit_idx,
                                                               float* __restrict__ hit_t, int32_t* err) {
     const int64_t n = src.d_count ? *src.d_count : src.n;
     int stack_ref[kBvhStack];
     float stack_t[kBvhStack];
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    for_each_ray(n, src.fetch, [&](int64_t k) {
         const HitRay r = load_hit_ray<AOS>(src, k);
         const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
         const float oix = r.ox * ix, oiy = r.oy * iy, oiz = r.oz * iz;
@@ -504,13 +527,14 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh_kernel(RaySrc src, BvhVie
         }
         hit_idx[k] = bi;
         if (hit_t) hit_t[k] = best;
-    }
+    });
 }
 
 cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, int32_t* hit_idx, float* hit_t,
                            int32_t* err, int sm_count, cudaStream_t s) {
     if (cap <= 0) return cudaSuccess;
-    const int grid = grid_for(cap, kBvhThreads, sm_count, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
+    const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh_kernel<false>), cap, sm_count)
+                                : grid_for(cap, kBvhThreads, sm_count, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
     if (rays.aos)
         hit_bvh_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
     else
@@ -533,14 +557,14 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_kernel(RaySrc src, Bvh4V
     const int64_t n = src.d_count ? *src.d_count : src.n;
     int stack_ref[kBvhStack];
     float stack_t[kBvhStack];
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    for_each_ray(n, src.fetch, [&](int64_t k) {
         const HitRay r = load_hit_ray<AOS>(src, k);
         float best;
         int32_t bi;
         bvh4_closest(r, bvh, stack_ref, stack_t, err, best, bi);
         hit_idx[k] = bi;
         if (hit_t) hit_t[k] = best;
-    }
+    });
 }
 
 
@@ -562,7 +586,8 @@ cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh
         prefer_l1(hit_bvh_kernel<false>);
         configured = true;
     }
-    const int grid = grid_for(cap, kBvhThreads, sm_count, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
+    const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh4_kernel<false>), cap, sm_count)
+                                : grid_for(cap, kBvhThreads, sm_count, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
     if (rays.aos)
         hit_bvh4_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
     else

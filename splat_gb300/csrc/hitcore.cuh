@@ -105,6 +105,28 @@ __device__ __forceinline__ float comp(const float4& v, int i) {
         rb = tr;                           \
     }
 
+// The rays [0, n) a thread traces.  With a work counter, each warp takes 32
+// consecutive rays at a time until the counter passes n (dynamic balance: a
+// warp whose rays finish early takes more, and the launch ends when the work
+// does); without one, a static grid-stride loop.
+template <class F>
+__device__ __forceinline__ void for_each_ray(int64_t n, unsigned long long* fetch, F&& body) {
+    if (fetch) {
+        const int lane = threadIdx.x & 31;
+        while (true) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(fetch, 32ull);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= (unsigned long long)n) break;
+            const int64_t k = (int64_t)base + lane;
+            if (k < n) body(k);
+        }
+    } else {
+        for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+            body(k);
+    }
+}
+
 // Closest hit of one ray in a four-wide BVH.  A node fetch (128 bytes)
 // tests four child boxes; hit children are sorted by entry distance, the
 // nearest is visited next and the others are pushed farthest first with

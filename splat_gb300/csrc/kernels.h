@@ -22,6 +22,7 @@ struct RaySrc {
     const splat_adray_t* aos;  // AoS rays (nullptr for SoA)
     const int64_t* d_count;    // active count on the device (SoA)
     int64_t n;                 // ray count when d_count is null
+    unsigned long long* fetch; // zeroed work counter: warps take rays 32 at a time (nullptr: grid-stride)
 };
 
 // Flattened BVH2 node (Aila & Laine 2009 layout): the boxes of both children
@@ -72,8 +73,17 @@ cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, 
                            int32_t* err, int sm_count, cudaStream_t s);
 cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh, int32_t* hit_idx, float* hit_t,
                             int32_t* err, int sm_count, cudaStream_t s);
+// grid of a work-counter traversal launch (one resident wave)
+int resident_grid(const void* kernel, int64_t cap, int sm_count);
 cudaError_t launch_refit4_level(Bvh4Node* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,
                                 const splat_ftri_t* ftri, float pad_abs, float pad_rel, cudaStream_t s);
+
+// GPU BVH rebuild (lbvh.cu): linear BVH over Morton-sorted centroids, written
+// as two-child and four-wide nodes with leaves of at most leaf_max triangles
+constexpr int kLbvhLeaf = 4;
+size_t lbvh_scratch_bytes(int64_t n_prims);
+cudaError_t launch_lbvh_build(const splat_ftri_t* ftri, int64_t n_tris, int leaf_max, void* scratch,
+                              BvhNode* nodes2, Bvh4Node* nodes4, int32_t* order, int sm_count, cudaStream_t s);
 
 // scene packing / refit
 cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, const int32_t* bvh_order,
@@ -206,6 +216,7 @@ struct BatchTickArgs {
     int32_t* err;
     int sm_count;
     bool any_brute;      // some item in flight uses the brute-force hitter (or has no BVH)
+    unsigned long long* fetch;  // zeroed work counter of this tick's hit kernel
 };
 
 cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s);

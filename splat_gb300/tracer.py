@@ -99,6 +99,10 @@ class Scene:
         """Per-frame geometry upload (repack + BVH refit) from a device FTri tensor."""
         L.check(L.load().splat_scene_update(self.handle, _ptr(d_tris), _stream()))
 
+    def rebuild(self, d_tris=None) -> None:
+        """Per-frame geometry upload with the BVH rebuilt on the GPU."""
+        L.check(L.load().splat_scene_rebuild(self.handle, _ptr(d_tris), _stream()))
+
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
             L.load().splat_scene_destroy(self._h)
