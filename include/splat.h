@@ -433,7 +433,10 @@ enum {
     SPLAT_TUNE_EVOLVE_BLOCKS_PER_SM = 2, /* evolve grid (default 8) */
     SPLAT_TUNE_SPLAT_BLOCKS_PER_SM = 3,  /* splat grid (default 8) */
     SPLAT_TUNE_SPLAT_AGGREGATE = 4,      /* splat sums samples per texel in shared memory first (default 0) */
-    SPLAT_TUNE_KEYS = 5
+    SPLAT_TUNE_BVH_PACKET = 5,           /* four-wide BVH warp packets: 0 never, 1 first bounce (default), 2 every bounce,
+                                            3 / 4 first bounce + per-warp choice by ray spread after (loose /
+                                            tight), 5 per-warp choice everywhere */
+    SPLAT_TUNE_KEYS = 6
 };
 splat_status_t splat_set_tuning(int32_t key, int32_t value);
 int32_t splat_get_tuning(int32_t key);

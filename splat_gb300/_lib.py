@@ -144,6 +144,7 @@ TUNE_BVH_BLOCKS_PER_SM = 1
 TUNE_EVOLVE_BLOCKS_PER_SM = 2
 TUNE_SPLAT_BLOCKS_PER_SM = 3
 TUNE_SPLAT_AGGREGATE = 4
+TUNE_BVH_PACKET = 5
 
 KERNEL_GENERATE = 0
 KERNEL_HIT_BRUTE = 1

@@ -76,7 +76,7 @@ struct Work {
     int64_t* counts;  // counts[b] = active rays after bounce b (b <= 64); counts[kSplatCount] = queued
 };
 constexpr int kSplatCount = 96;
-constexpr int kFetchBase = 128;  // counts[kFetchBase + b]: work counter of bounce b's hit launch
+constexpr int kFetchBase = 128;  // counts[kFetchBase + b]: work counter of bounce b's hit launch (b <= 64)
 constexpr size_t kCounterBytes = 2048;
 
 size_t work_bytes(int64_t cap) {
@@ -95,6 +95,20 @@ Work carve_work(void* ws, int64_t cap) {
     p += align_up(8 * (size_t)cap);
     w.counts = reinterpret_cast<int64_t*>(p);
     return w;
+}
+
+// Traversal form of bounce b (1-based) under the SPLAT_TUNE_BVH_PACKET knob:
+// 0 one ray per lane; 1 warp packets; 2, 3 per-warp choice by ray spread
+// (loose, tight thresholds).
+int32_t packet_for(int32_t b) {
+    switch (g_tune[SPLAT_TUNE_BVH_PACKET]) {
+        case 1: return b == 1 ? 1 : 0;
+        case 2: return 1;
+        case 3: return b == 1 ? 1 : 2;
+        case 4: return b == 1 ? 1 : 3;
+        case 5: return 2;
+        default: return 0;
+    }
 }
 
 bool valid_material(const splat_material_t* m) {
@@ -503,6 +517,7 @@ splat_status_t splat_next_hit(const splat_scene_t* scene, int32_t hitter, const 
     RaySrc src{};
     src.aos = d_rays;
     src.n = n_rays;
+    src.packet = packet_for(2);
     return hit_any(scene, hitter, src, n_rays, d_hit_idx, d_hit_t, nullptr, reinterpret_cast<cudaStream_t>(stream));
 }
 
@@ -579,7 +594,7 @@ splat_status_t splat_run_evolution(const splat_scene_t* scene, int32_t hitter, s
     ea.aos = d_rays;
     for (int32_t b = 1; b <= depth; ++b) {
         RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0,
-                   reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b])};
+                   reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b]), packet_for(b)};
         splat_status_t rc = hit_any(scene, hitter, src, n_rays, w.hit, nullptr, w.tmp, st);
         if (rc != SPLAT_OK) return rc;
         ea.in = cur;
@@ -692,7 +707,7 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
     RaySoA cur = w.a, nxt = w.b;
     for (int32_t b = 1; b <= P->depth; ++b) {
         RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0,
-                   reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b])};
+                   reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b]), packet_for(b)};
         rc = hit_any(scene, P->hitter, src, cnt, w.hit, nullptr, w.tmp, st);
         if (rc != SPLAT_OK) return rc;
         ea.in = cur;
@@ -759,6 +774,8 @@ splat_status_t splat_set_tuning(int32_t key, int32_t value) {
     if (key < 0 || key >= SPLAT_TUNE_KEYS) return fail(SPLAT_ERR_INVALID, "set_tuning: unknown key");
     if (key == SPLAT_TUNE_SPLAT_AGGREGATE) {
         if (value != 0 && value != 1) return fail(SPLAT_ERR_INVALID, "set_tuning: aggregate must be 0 or 1");
+    } else if (key == SPLAT_TUNE_BVH_PACKET) {
+        if (value < 0 || value > 5) return fail(SPLAT_ERR_INVALID, "set_tuning: packet mode must be 0..5");
     } else if (value < 1 || value > 256) {
         return fail(SPLAT_ERR_INVALID, "set_tuning: value must be 1..256");
     }
@@ -1553,7 +1570,7 @@ splat_status_t splat_render_camera(const splat_scene_t* scene, const splat_shade
     RaySoA cur = w.a, nxt = w.b;
     for (int32_t b = 1; b <= P->depth; ++b) {
         RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0,
-                   reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b])};
+                   reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b]), packet_for(b)};
         rc = hit_any(scene, P->hitter, src, cnt, w.hit, nullptr, w.tmp, st);
         if (rc != SPLAT_OK) return rc;
         ea.in = cur;

@@ -258,11 +258,11 @@ cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s) {
     if (a.cap_rays > 0) {
         if (a.any_brute)
             batch_hit_kernel<true><<<resident_grid(reinterpret_cast<const void*>(batch_hit_kernel<true>), a.cap_rays,
-                                                   a.sm_count),
+                                                   a.sm_count, 128, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]),
                                      128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch);
         else
             batch_hit_kernel<false><<<resident_grid(reinterpret_cast<const void*>(batch_hit_kernel<false>), a.cap_rays,
-                                                    a.sm_count),
+                                                    a.sm_count, 128, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]),
                                       128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch);
         ++g_launches;
         batch_evolve_kernel<<<grid_cap(a.cap_rays, kBatchThreads, a.sm_count, 8), kBatchThreads, 0, s>>>(

@@ -307,4 +307,48 @@ __device__ __forceinline__ float fresnel_draw(uint64_t seed, uint32_t id, uint32
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
+// The rays [0, n) a thread traces.  With a work counter, each warp takes 32
+// consecutive rays at a time until the counter passes n (dynamic balance: a
+// warp whose rays finish early takes more, and the launch ends when the work
+// does); without one, a static grid-stride loop.
+template <class F>
+__device__ __forceinline__ void for_each_ray(int64_t n, unsigned long long* fetch, F&& body) {
+    if (fetch) {
+        const int lane = threadIdx.x & 31;
+        while (true) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(fetch, 32ull);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= (unsigned long long)n) break;
+            const int64_t k = (int64_t)base + lane;
+            if (k < n) body(k);
+        }
+    } else {
+        for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+            body(k);
+    }
+}
+
+// Warp-uniform batches of 32 consecutive rays [base, base + 32) (lanes past
+// n idle inside the body): from a work counter, or a static grid-stride over
+// warps.  Every lane of the warp runs the body, so it may use warp votes.
+template <class F>
+__device__ __forceinline__ void for_each_warp_batch(int64_t n, unsigned long long* fetch, F&& body) {
+    const int lane = threadIdx.x & 31;
+    if (fetch) {
+        while (true) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(fetch, 32ull);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= (unsigned long long)n) break;
+            body((int64_t)base);
+        }
+    } else {
+        const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+        for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += stride)
+            body(base);
+    }
+}
+
+
 }  // namespace splat

@@ -24,7 +24,7 @@
 namespace splat {
 
 thread_local int64_t g_launches = 0;
-int32_t g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0};
+int32_t g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1};
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + bulk copy (sm_90+ async proxy)
@@ -415,10 +415,10 @@ cudaError_t launch_hit_brute_ntris_static(const splat_adray_t* rays, int64_t n_r
 // ---------------------------------------------------------------------------
 constexpr int kBvhThreads = 128;
 
-// Grid of a work-counter launch: as many 128-thread blocks as stay resident
-// together (capped by the blocks-per-SM knob and by the work), so the launch
-// is one wave that drains the counter.
-int resident_grid(const void* kernel, int64_t cap, int sm_count) {
+// Grid of a work-counter launch: as many blocks as stay resident together
+// (capped by a blocks-per-SM knob and by the work), so the launch is one
+// wave that drains the counter.
+int resident_grid(const void* kernel, int64_t cap, int sm_count, int threads, int max_per_sm) {
     static std::mutex mu;
     static std::unordered_map<const void*, int> occ;
     int per_sm = 0;
@@ -427,14 +427,14 @@ int resident_grid(const void* kernel, int64_t cap, int sm_count) {
         auto it = occ.find(kernel);
         if (it == occ.end()) {
             int nb = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kBvhThreads, 0) != cudaSuccess || nb < 1)
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, 0) != cudaSuccess || nb < 1)
                 nb = 4;
             it = occ.emplace(kernel, nb).first;
         }
         per_sm = it->second;
     }
-    if (per_sm > g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]) per_sm = g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM];
-    return grid_for(cap, kBvhThreads, sm_count, per_sm);
+    if (per_sm > max_per_sm) per_sm = max_per_sm;
+    return grid_for(cap, threads, sm_count, per_sm);
 }
 
 template <bool AOS>
@@ -533,7 +533,8 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh_kernel(RaySrc src, BvhVie
 cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, int32_t* hit_idx, float* hit_t,
                            int32_t* err, int sm_count, cudaStream_t s) {
     if (cap <= 0) return cudaSuccess;
-    const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh_kernel<false>), cap, sm_count)
+    const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh_kernel<false>), cap, sm_count,
+                                                kBvhThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM])
                                 : grid_for(cap, kBvhThreads, sm_count, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
     if (rays.aos)
         hit_bvh_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
@@ -568,6 +569,78 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_kernel(RaySrc src, Bvh4V
 }
 
 
+// Spread of a warp's rays, max over axes of (max - min) of a coordinate.
+__device__ __forceinline__ float warp_spread(float a, float b, float c) {
+    float m = 0.0f;
+    const float v[3] = {a, b, c};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float lo = v[i], hi = v[i];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        m = fmaxf(m, hi - lo);
+    }
+    return m;
+}
+
+// Packet form: each warp traverses its 32 rays together (bvh4_closest_packet)
+// on a shared-memory stack.  ADAPT: per warp, packets only when its rays are
+// nearly parallel (direction spread <= dir_spread) and close together (origin
+// spread <= org_spread x the scene's extent); otherwise one ray per lane.
+template <bool AOS, bool ADAPT>
+__global__ void __launch_bounds__(kBvhThreads) hit_bvh4_packet_kernel(RaySrc src, Bvh4View bvh,
+                                                                      int32_t* __restrict__ hit_idx,
+                                                                      float* __restrict__ hit_t, int32_t* err,
+                                                                      float dir_spread, float org_spread) {
+    __shared__ int s_stack[kBvhThreads / 32][kPacketStack];
+    int* stack = s_stack[threadIdx.x >> 5];
+    const int64_t n = src.d_count ? *src.d_count : src.n;
+    const int lane = threadIdx.x & 31;
+    float extent = 0.0f;
+    if (ADAPT) {
+        const Bvh4Node& root = bvh.nodes[0];
+        const float4 lx = __ldg(&root.lox), hx = __ldg(&root.hix), ly = __ldg(&root.loy), hy = __ldg(&root.hiy);
+        const float4 lz = __ldg(&root.loz), hz = __ldg(&root.hiz);
+        const int nc = __ldg(&root.meta.x);
+        float lo[3] = {lx.x, ly.x, lz.x}, hi[3] = {hx.x, hy.x, hz.x};
+        for (int i = 1; i < nc; ++i) {
+            lo[0] = fminf(lo[0], comp(lx, i));
+            lo[1] = fminf(lo[1], comp(ly, i));
+            lo[2] = fminf(lo[2], comp(lz, i));
+            hi[0] = fmaxf(hi[0], comp(hx, i));
+            hi[1] = fmaxf(hi[1], comp(hy, i));
+            hi[2] = fmaxf(hi[2], comp(hz, i));
+        }
+        extent = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+    }
+    int stack_ref[ADAPT ? kBvhStack : 1];
+    float stack_t[ADAPT ? kBvhStack : 1];
+    for_each_warp_batch(n, src.fetch, [&](int64_t base) {
+        const int64_t k = base + lane;
+        const bool valid = k < n;
+        const HitRay r = load_hit_ray<AOS>(src, valid ? k : base);
+        float best;
+        int32_t bi;
+        bool packet = true;
+        if (ADAPT) {
+            const float ds = warp_spread(r.dx, r.dy, r.dz), os = warp_spread(r.ox, r.oy, r.oz);
+            packet = ds <= dir_spread && os <= org_spread * extent;
+        }
+        if (packet) {
+            bvh4_closest_packet(r, valid, bvh, stack, err, best, bi);
+        } else if (ADAPT && valid) {
+            bvh4_closest(r, bvh, stack_ref, stack_t, err, best, bi);
+        }
+        if (valid) {
+            hit_idx[k] = bi;
+            if (hit_t) hit_t[k] = best;
+        }
+    });
+}
+
 // The traversal kernels use no shared memory: give the whole L1/shared
 // array to L1, where the upper BVH levels and hot hit records live.
 template <class K>
@@ -586,7 +659,32 @@ cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh
         prefer_l1(hit_bvh_kernel<false>);
         configured = true;
     }
-    const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh4_kernel<false>), cap, sm_count)
+    if (rays.packet) {
+        // packet = 1: every warp; 2, 3: per warp by ray spread (loose, tight)
+        const float ds = rays.packet == 2 ? 0.3f : 0.1f, os = rays.packet == 2 ? 0.05f : 0.01f;
+        const int knob = g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM];
+        if (rays.packet == 1) {
+            const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh4_packet_kernel<false, false>),
+                                                        cap, sm_count, kBvhThreads, knob)
+                                        : grid_for(cap, kBvhThreads, sm_count, knob);
+            if (rays.aos)
+                hit_bvh4_packet_kernel<true, false><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, ds, os);
+            else
+                hit_bvh4_packet_kernel<false, false><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, ds, os);
+        } else {
+            const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh4_packet_kernel<false, true>),
+                                                        cap, sm_count, kBvhThreads, knob)
+                                        : grid_for(cap, kBvhThreads, sm_count, knob);
+            if (rays.aos)
+                hit_bvh4_packet_kernel<true, true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, ds, os);
+            else
+                hit_bvh4_packet_kernel<false, true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, ds, os);
+        }
+        ++g_launches;
+        return cudaGetLastError();
+    }
+    const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh4_kernel<false>), cap, sm_count,
+                                                kBvhThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM])
                                 : grid_for(cap, kBvhThreads, sm_count, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
     if (rays.aos)
         hit_bvh4_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);

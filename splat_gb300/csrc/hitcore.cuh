@@ -105,28 +105,6 @@ __device__ __forceinline__ float comp(const float4& v, int i) {
         rb = tr;                           \
     }
 
-// The rays [0, n) a thread traces.  With a work counter, each warp takes 32
-// consecutive rays at a time until the counter passes n (dynamic balance: a
-// warp whose rays finish early takes more, and the launch ends when the work
-// does); without one, a static grid-stride loop.
-template <class F>
-__device__ __forceinline__ void for_each_ray(int64_t n, unsigned long long* fetch, F&& body) {
-    if (fetch) {
-        const int lane = threadIdx.x & 31;
-        while (true) {
-            unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(fetch, 32ull);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base >= (unsigned long long)n) break;
-            const int64_t k = (int64_t)base + lane;
-            if (k < n) body(k);
-        }
-    } else {
-        for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
-            body(k);
-    }
-}
-
 // Closest hit of one ray in a four-wide BVH.  A node fetch (128 bytes)
 // tests four child boxes; hit children are sorted by entry distance, the
 // nearest is visited next and the others are pushed farthest first with
@@ -221,6 +199,103 @@ __device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bv
     bi_out = bi;
 }
 #undef SPLAT_CSWAP
+
+// Packet traversal of a four-wide BVH: the 32 rays of a warp walk one
+// shared stack.  A child is entered when any lane's ray enters its box at or
+// before that lane's best hit; children are visited in the order of the
+// warp's smallest entry distance (a __reduce_min over order-preserving
+// codes), so every decision is warp-uniform and the node loads are
+// broadcasts.  Every lane tests every triangle of a visited leaf against its
+// own ray.  Each lane still ends with the lexicographic (t, index) minimum
+// over every triangle whose padded box its ray enters at or before its best
+// hit, so the result equals the per-ray traversal and brute force.  For
+// coherent rays (a light's primary rays, refraction through smooth glass)
+// the union of the lanes' paths is little more than one ray's path, and the
+// warp runs it with all lanes busy.  stack: kPacketStack ints shared by the
+// warp; every lane writes every entry (same value), so no warp barrier.
+constexpr int kPacketStack = 128;
+
+__device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid, const Bvh4View& bvh, int* stack,
+                                                    int32_t* err, float& best_out, int32_t& bi_out) {
+    const float kInf = __int_as_float(0x7f800000);
+    const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
+    const float oix = r.ox * ix, oiy = r.oy * iy, oiz = r.oz * iz;
+    float best = kInf;
+    int32_t bi = 1;
+    int sp = 0;
+    int ref = 0;
+    while (true) {
+        if (ref >= 0) {
+            const Bvh4Node* nd = bvh.nodes + ref;
+            const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix);
+            const float4 ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
+            const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+            const int4 c = __ldg(&nd->c);
+            const int nc = __ldg(&nd->meta.x);
+            unsigned u[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float a0 = fmaf(comp(lx, i), ix, -oix), b0 = fmaf(comp(hx, i), ix, -oix);
+                const float a1 = fmaf(comp(ly, i), iy, -oiy), b1 = fmaf(comp(hy, i), iy, -oiy);
+                const float a2 = fmaf(comp(lz, i), iz, -oiz), b2 = fmaf(comp(hz, i), iz, -oiz);
+                const float tmin = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fminf(a2, b2));
+                const float tmax = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fmaxf(a2, b2));
+                const bool h = valid & (i < nc) & (tmin <= tmax) & (tmax >= 0.0f) & (tmin <= best);
+                u[i] = __reduce_min_sync(0xffffffffu, h ? monotonic_u32(tmin) : 0xffffffffu);
+            }
+            unsigned k0 = u[0], k1 = u[1], k2 = u[2], k3 = u[3];
+            int r0 = c.x, r1 = c.y, r2 = c.z, r3 = c.w;
+#define SPLAT_USWAP(ka, ra, kb, rb)          \
+    if (kb < ka) {                           \
+        const unsigned tk = ka;              \
+        ka = kb;                             \
+        kb = tk;                             \
+        const int tr = ra;                   \
+        ra = rb;                             \
+        rb = tr;                             \
+    }
+            SPLAT_USWAP(k0, r0, k1, r1);
+            SPLAT_USWAP(k2, r2, k3, r3);
+            SPLAT_USWAP(k0, r0, k2, r2);
+            SPLAT_USWAP(k1, r1, k3, r3);
+            SPLAT_USWAP(k1, r1, k2, r2);
+#undef SPLAT_USWAP
+            if (k0 != 0xffffffffu) {
+                if (sp + 3 <= kPacketStack) {
+                    if (k3 != 0xffffffffu) stack[sp++] = r3;
+                    if (k2 != 0xffffffffu) stack[sp++] = r2;
+                    if (k1 != 0xffffffffu) stack[sp++] = r1;
+                } else if (threadIdx.x % 32 == 0) {
+                    atomicOr(err, 2);
+                }
+                ref = r0;
+                continue;
+            }
+        } else {
+            const int enc = ~ref;
+            const int first = enc >> 4;
+            const int count = (enc & 15) + 1;
+            for (int j = 0; j < count; ++j) {
+                const TriHit* h = bvh.tris + first + j;
+                float num, den;
+                const bool cand = valid && tri_candidate(__ldg(&h->n_nv), r, best, num, den);
+                if (!cand) continue;
+                const float4 q1 = __ldg(&h->a_idx);
+                const int32_t idx = __float_as_int(q1.w);
+                bool inside;
+                const float t = tri_t_from(num, den, q1, __ldg(&h->e0), __ldg(&h->e1), __ldg(&h->inv), r, inside);
+                if (inside & (t > 0.0f) & (idx != r.ig) & ((t < best) | ((t == best) & (idx < bi)))) {
+                    best = t;
+                    bi = idx;
+                }
+            }
+        }
+        if (sp == 0) break;
+        ref = stack[--sp];
+    }
+    best_out = best;
+    bi_out = bi;
+}
 
 // Closest hit of one ray over hit records in reference-index order (the
 // per-ray form of the brute-force hitter; strict < keeps the smaller index).

@@ -23,6 +23,7 @@ struct RaySrc {
     const int64_t* d_count;    // active count on the device (SoA)
     int64_t n;                 // ray count when d_count is null
     unsigned long long* fetch; // zeroed work counter: warps take rays 32 at a time (nullptr: grid-stride)
+    int32_t packet;            // four-wide BVH: warp packet traversal (1) or one ray per lane (0)
 };
 
 // Flattened BVH2 node (Aila & Laine 2009 layout): the boxes of both children
@@ -74,7 +75,7 @@ cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, 
 cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh, int32_t* hit_idx, float* hit_t,
                             int32_t* err, int sm_count, cudaStream_t s);
 // grid of a work-counter traversal launch (one resident wave)
-int resident_grid(const void* kernel, int64_t cap, int sm_count);
+int resident_grid(const void* kernel, int64_t cap, int sm_count, int threads, int max_per_sm);
 cudaError_t launch_refit4_level(Bvh4Node* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,
                                 const splat_ftri_t* ftri, float pad_abs, float pad_rel, cudaStream_t s);
 

@@ -161,3 +161,42 @@ def test_refit_after_geometry_change(torch_cuda):
         hit, t = _hits(tracer, scene, hitter, rays)
         assert np.array_equal(hit, o_hit), f"hitter {hitter}"
         assert np.array_equal(t.view(np.uint32), o_t.view(np.uint32))
+
+
+def test_packet_traversal_matches_oracle(torch_cuda):
+    """The warp-packet four-wide traversal (SPLAT_TUNE_BVH_PACKET = 2) gives
+    the oracle's hits bit for bit on coherent and incoherent rays, through
+    the plugin entry and the fused step."""
+    from splat_gb300 import _lib as L
+    from splat_gb300 import scenes as S
+    from splat_gb300 import tracer
+
+    lib = L.load()
+    old = lib.splat_get_tuning(L.TUNE_BVH_PACKET)
+    tris, fd = small_scene(3, 0.05)
+    scene = tracer.Scene(tris, fd, bvh=True)
+    light = S.hemisphere_light(2, 96, 1.05)
+    coherent = O.rays_from_light(light, 1, (0, 1, 550.0, 550.0), 3)
+    incoherent = random_rays(5000, 17, tris.shape[0])
+    try:
+        L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, 2))
+        for rays in (coherent, incoherent, incoherent[:37]):
+            o_hit, o_t = O.next_hit(rays, tris)
+            hit, t = _hits(tracer, scene, tracer.BVH, rays)
+            assert np.array_equal(hit, o_hit) and np.array_equal(t.view(np.uint32), o_t.view(np.uint32))
+        scene.rebuild()
+        hit, t = _hits(tracer, scene, tracer.BVH, incoherent)
+        o_hit, o_t = O.next_hit(incoherent, tris)
+        assert np.array_equal(hit, o_hit)
+        wl = S.realtime(light=S.scaled_light(S.realtime().light, 384))
+        sc = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
+        maps = []
+        for mode in range(6):
+            L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, mode))
+            maps.append(tracer.trace_forward(wl, scene=sc).tex.cpu().numpy())
+        assert all(np.array_equal(maps[0], m) for m in maps[1:]) and maps[0].sum() > 0
+        L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, 5))
+        hit, t = _hits(tracer, scene, tracer.BVH, incoherent)
+        assert np.array_equal(hit, o_hit)
+    finally:
+        L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, old))
