@@ -167,12 +167,11 @@ struct splat_scene {
     int64_t n_nodes = 0;
     TriHit* d_bvh = nullptr;
     int32_t* d_order = nullptr;
-    int32_t* d_levels = nullptr;
-    std::vector<int64_t> level_off;
+    int32_t* d_links = nullptr;  // refit links of the two-child tree
     Bvh4Node* d_nodes4 = nullptr;
     int64_t n_nodes4 = 0;
-    int32_t* d_levels4 = nullptr;
-    std::vector<int64_t> level4_off;
+    int32_t* d_links4 = nullptr;  // refit links of the four-wide tree
+    unsigned* d_flags = nullptr;  // refit arrival counts
     int depth = 0, max_leaf = 0;
     int64_t leaves = 0;
     float pad_abs = 0.f, pad_rel = 0.f;
@@ -194,9 +193,10 @@ static void scene_free(splat_scene* s) {
     cudaFree(s->d_nodes);
     cudaFree(s->d_bvh);
     cudaFree(s->d_order);
-    cudaFree(s->d_levels);
+    cudaFree(s->d_links);
     cudaFree(s->d_nodes4);
-    cudaFree(s->d_levels4);
+    cudaFree(s->d_links4);
+    cudaFree(s->d_flags);
     cudaFree(s->d_err);
     cudaFree(s->d_lbvh);
     delete s;
@@ -212,20 +212,15 @@ static splat_status_t scene_pack(splat_scene* s, cudaStream_t st) {
     ProfScope ps(SPLAT_KERNEL_AUX, st);
     cudaError_t e = launch_pack_hits(s->d_ftri, s->n_tris, s->d_brute, s->d_order, s->d_bvh, st);
     if (e != cudaSuccess) return cuda_fail(e, "pack hit records");
-    if (s->d_nodes) {
-        for (size_t l = 0; l + 1 < s->level_off.size(); ++l) {
-            const int64_t a = s->level_off[l], b = s->level_off[l + 1];
-            e = launch_refit_level(s->d_nodes, s->d_levels + a, b - a, s->d_bvh, s->d_ftri, s->pad_abs, s->pad_rel, st);
-            if (e != cudaSuccess) return cuda_fail(e, "BVH refit");
-        }
+    if (s->d_nodes && s->d_links) {
+        e = launch_refit_tree(s->d_nodes, false, s->n_nodes, s->d_links, s->d_flags, s->d_bvh, s->d_ftri, s->pad_abs,
+                              s->pad_rel, st);
+        if (e != cudaSuccess) return cuda_fail(e, "BVH refit");
     }
-    if (s->d_nodes4) {
-        for (size_t l = 0; l + 1 < s->level4_off.size(); ++l) {
-            const int64_t a = s->level4_off[l], b = s->level4_off[l + 1];
-            e = launch_refit4_level(s->d_nodes4, s->d_levels4 + a, b - a, s->d_bvh, s->d_ftri, s->pad_abs, s->pad_rel,
-                                    st);
-            if (e != cudaSuccess) return cuda_fail(e, "BVH4 refit");
-        }
+    if (s->d_nodes4 && s->d_links4) {
+        e = launch_refit_tree(s->d_nodes4, true, s->n_nodes4, s->d_links4, s->d_flags, s->d_bvh, s->d_ftri, s->pad_abs,
+                              s->pad_rel, st);
+        if (e != cudaSuccess) return cuda_fail(e, "BVH4 refit");
     }
     return SPLAT_OK;
 }
@@ -293,14 +288,13 @@ splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris,
         chk(dalloc(&s->d_nodes, sizeof(BvhNode) * bvh.nodes.size(), s->bytes));
         chk(dalloc(&s->d_bvh, sizeof(TriHit) * (size_t)s->n_recs, s->bytes));
         chk(dalloc(&s->d_order, sizeof(int32_t) * bvh.order.size(), s->bytes));
-        chk(dalloc(&s->d_levels, sizeof(int32_t) * bvh.level_nodes.size(), s->bytes));
+        chk(dalloc(&s->d_links, sizeof(int32_t) * bvh.links.size(), s->bytes));
         s->n_nodes4 = (int64_t)bvh.nodes4.size();
         s->cap_nodes = s->n_nodes;
         s->cap_nodes4 = s->n_nodes4;
         chk(dalloc(&s->d_nodes4, sizeof(Bvh4Node) * bvh.nodes4.size(), s->bytes));
-        chk(dalloc(&s->d_levels4, sizeof(int32_t) * bvh.level4_nodes.size(), s->bytes));
-        s->level4_off = bvh.level4_off;
-        s->level_off = bvh.level_off;
+        chk(dalloc(&s->d_links4, sizeof(int32_t) * bvh.links4.size(), s->bytes));
+        chk(dalloc(&s->d_flags, sizeof(unsigned) * std::max(bvh.nodes.size(), bvh.nodes4.size()), s->bytes));
         s->depth = bvh.depth;
         s->max_leaf = bvh.max_leaf;
         s->leaves = bvh.leaves;
@@ -318,11 +312,11 @@ splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris,
                             st));
         chk(cudaMemcpyAsync(s->d_order, bvh.order.data(), sizeof(int32_t) * bvh.order.size(), cudaMemcpyHostToDevice,
                             st));
-        chk(cudaMemcpyAsync(s->d_levels, bvh.level_nodes.data(), sizeof(int32_t) * bvh.level_nodes.size(),
-                            cudaMemcpyHostToDevice, st));
+        chk(cudaMemcpyAsync(s->d_links, bvh.links.data(), sizeof(int32_t) * bvh.links.size(), cudaMemcpyHostToDevice,
+                            st));
         chk(cudaMemcpyAsync(s->d_nodes4, bvh.nodes4.data(), sizeof(Bvh4Node) * bvh.nodes4.size(),
                             cudaMemcpyHostToDevice, st));
-        chk(cudaMemcpyAsync(s->d_levels4, bvh.level4_nodes.data(), sizeof(int32_t) * bvh.level4_nodes.size(),
+        chk(cudaMemcpyAsync(s->d_links4, bvh.links4.data(), sizeof(int32_t) * bvh.links4.size(),
                             cudaMemcpyHostToDevice, st));
     }
     if (e == cudaSuccess) chk(launch_pack_hits(s->d_ftri, n_tris, s->d_brute, s->d_order, s->d_bvh, st));

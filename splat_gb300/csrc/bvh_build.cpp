@@ -272,16 +272,18 @@ bool build_bvh(const splat_ftri_t* tris, int64_t n_tris, BvhHost& out, std::stri
     out.order.resize((size_t)np);
     for (int64_t j = 0; j < np; ++j) out.order[(size_t)j] = P[(size_t)j].idx;
 
-    // refit schedule: inner nodes grouped by depth, deepest level first
     int maxd = 0;
     for (int d : depth_of) maxd = std::max(maxd, d);
     out.depth = maxd + 1;
-    out.level_off.assign(1, 0);
-    for (int d = maxd; d >= 0; --d) {
-        for (size_t q = 0; q < depth_of.size(); ++q)
-            if (depth_of[q] == d) out.level_nodes.push_back((int32_t)q);
-        out.level_off.push_back((int64_t)out.level_nodes.size());
-    }
+    // refit links: parent of each node, then its number of inner children
+    out.links.assign(2 * out.nodes.size(), 0);
+    out.links[0] = -1;
+    for (size_t q = 0; q < out.nodes.size(); ++q)
+        for (int c : {out.nodes[q].c.x, out.nodes[q].c.y})
+            if (c >= 0 && c != (int)q) {
+                out.links[(size_t)c] = (int32_t)q;
+                out.links[out.nodes.size() + q] += 1;
+            }
     if (out.depth + 1 >= kBvhStack) {
         err = "BVH deeper than the traversal stack";
         return false;
@@ -343,11 +345,16 @@ bool build_bvh(const splat_ftri_t* tris, int64_t n_tris, BvhHost& out, std::stri
     int maxd4 = 0;
     for (int d : depth4_of) maxd4 = std::max(maxd4, d);
     out.depth4 = maxd4 + 1;
-    out.level4_off.assign(1, 0);
-    for (int d = maxd4; d >= 0; --d) {
-        for (size_t q = 0; q < depth4_of.size(); ++q)
-            if (depth4_of[q] == d) out.level4_nodes.push_back((int32_t)q);
-        out.level4_off.push_back((int64_t)out.level4_nodes.size());
+    out.links4.assign(2 * out.nodes4.size(), 0);
+    out.links4[0] = -1;
+    for (size_t q = 0; q < out.nodes4.size(); ++q) {
+        const Bvh4Node& f = out.nodes4[q];
+        const int refs[4] = {f.c.x, f.c.y, f.c.z, f.c.w};
+        for (int i = 0; i < f.meta.x; ++i)
+            if (refs[i] >= 0) {
+                out.links4[(size_t)refs[i]] = (int32_t)q;
+                out.links4[out.nodes4.size() + q] += 1;
+            }
     }
     if (3 * out.depth4 + 1 >= kBvhStack) {
         err = "four-wide BVH deeper than the traversal stack";

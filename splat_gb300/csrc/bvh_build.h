@@ -11,16 +11,14 @@ namespace splat {
 struct BvhHost {
     std::vector<BvhNode> nodes;
     std::vector<int32_t> order;        // reference index of each BVH-ordered record
-    std::vector<int32_t> level_nodes;  // inner nodes grouped by depth, deepest first
-    std::vector<int64_t> level_off;
+    std::vector<int32_t> links;  // refit: parent per node (-1 root), then inner-child count per node
     int depth = 0;
     int max_leaf = 0;
     int64_t leaves = 0;
     float pad_abs = 0.f, pad_rel = 0.f;
     // four-wide tree collapsed from the binary one (same leaves)
     std::vector<Bvh4Node> nodes4;
-    std::vector<int32_t> level4_nodes;
-    std::vector<int64_t> level4_off;
+    std::vector<int32_t> links4;
     int depth4 = 0;
 };
 

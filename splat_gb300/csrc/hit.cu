@@ -720,58 +720,6 @@ cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* b
     return cudaGetLastError();
 }
 
-// Box of one child reference.  Leaf boxes are the padded vertex boxes of
-// their triangles; inner boxes are the union of the child node's two boxes.
-__device__ __forceinline__ void child_box(const BvhNode* nodes, int ref, const TriHit* recs,
-                                          const splat_ftri_t* ftri, float pad_abs, float pad_rel, float lo[3],
-                                          float hi[3]) {
-    for (int a = 0; a < 3; ++a) {
-        lo[a] = __int_as_float(0x7f800000);
-        hi[a] = -__int_as_float(0x7f800000);
-    }
-    if (ref >= 0) {
-        const BvhNode& nd = nodes[ref];
-        lo[0] = fminf(nd.x.x, nd.x.z);
-        hi[0] = fmaxf(nd.x.y, nd.x.w);
-        lo[1] = fminf(nd.y.x, nd.y.z);
-        hi[1] = fmaxf(nd.y.y, nd.y.w);
-        lo[2] = fminf(nd.z.x, nd.z.z);
-        hi[2] = fmaxf(nd.z.y, nd.z.w);
-        return;
-    }
-    const int enc = ~ref;
-    const int first = enc >> 4, count = (enc & 15) + 1;
-    for (int j = 0; j < count; ++j) {
-        const int32_t idx = __float_as_int(recs[first + j].a_idx.w);
-        const float* p = ftri[idx - 1].v[1];
-        float tl[3], th[3];
-        for (int a = 0; a < 3; ++a) {
-            tl[a] = fminf(fminf(p[a], p[3 + a]), p[6 + a]);
-            th[a] = fmaxf(fmaxf(p[a], p[3 + a]), p[6 + a]);
-        }
-        const float dx = th[0] - tl[0], dy = th[1] - tl[1], dz = th[2] - tl[2];
-        const float pad = pad_abs + pad_rel * sqrtf(dx * dx + dy * dy + dz * dz);
-        for (int a = 0; a < 3; ++a) {
-            lo[a] = fminf(lo[a], tl[a] - pad);
-            hi[a] = fmaxf(hi[a], th[a] + pad);
-        }
-    }
-}
-
-__global__ void refit_level_kernel(BvhNode* nodes, const int32_t* __restrict__ level_nodes, int64_t n_level,
-                                   const TriHit* __restrict__ recs, const splat_ftri_t* __restrict__ ftri,
-                                   float pad_abs, float pad_rel) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n_level; q += (int64_t)gridDim.x * blockDim.x) {
-        BvhNode& nd = nodes[level_nodes[q]];
-        float l0[3], h0[3], l1[3], h1[3];
-        child_box(nodes, nd.c.x, recs, ftri, pad_abs, pad_rel, l0, h0);
-        child_box(nodes, nd.c.y, recs, ftri, pad_abs, pad_rel, l1, h1);
-        nd.x = make_float4(l0[0], h0[0], l1[0], h1[0]);
-        nd.y = make_float4(l0[1], h0[1], l1[1], h1[1]);
-        nd.z = make_float4(l0[2], h0[2], l1[2], h1[2]);
-    }
-}
-
 __device__ __forceinline__ void leaf_box(int ref, const TriHit* recs, const splat_ftri_t* ftri, float pad_abs,
                                          float pad_rel, float lo[3], float hi[3]) {
     const int enc = ~ref;
@@ -793,60 +741,115 @@ __device__ __forceinline__ void leaf_box(int ref, const TriHit* recs, const spla
     }
 }
 
-__global__ void refit4_level_kernel(Bvh4Node* nodes, const int32_t* __restrict__ level_nodes, int64_t n_level,
-                                    const TriHit* __restrict__ recs, const splat_ftri_t* __restrict__ ftri,
-                                    float pad_abs, float pad_rel) {
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n_level; q += (int64_t)gridDim.x * blockDim.x) {
-        Bvh4Node& nd = nodes[level_nodes[q]];
-        const int nc = nd.meta.x;
-        float lo[3][4], hi[3][4];
-        const int refs[4] = {nd.c.x, nd.c.y, nd.c.z, nd.c.w};
-        for (int i = 0; i < 4; ++i) {
-            float l[3] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000)};
-            float h[3] = {-l[0], -l[0], -l[0]};
-            if (i < nc) {
-                if (refs[i] >= 0) {
-                    const Bvh4Node& ch = nodes[refs[i]];
-                    for (int j = 0; j < ch.meta.x; ++j) {
-                        l[0] = fminf(l[0], comp(ch.lox, j));
-                        h[0] = fmaxf(h[0], comp(ch.hix, j));
-                        l[1] = fminf(l[1], comp(ch.loy, j));
-                        h[1] = fmaxf(h[1], comp(ch.hiy, j));
-                        l[2] = fminf(l[2], comp(ch.loz, j));
-                        h[2] = fmaxf(h[2], comp(ch.hiz, j));
-                    }
-                } else {
-                    leaf_box(refs[i], recs, ftri, pad_abs, pad_rel, l, h);
+// One-launch refit: the threads of the nodes whose children are all leaves
+// start; each node's box union is written by the last of its inner children
+// to finish (atomic arrival count against its number of inner children), so
+// the tree is refit bottom-up without a launch per level.  links[q] =
+// parent of node q (-1: root), links[n + q] = its number of inner children.
+// Child nodes written by other threads are read through L2 (__ldcg).
+__device__ __forceinline__ float4 ldcg4(const float4* p) { return __ldcg(p); }
+
+__device__ __forceinline__ void refit2_node(BvhNode* nodes, int q, const TriHit* recs, const splat_ftri_t* ftri,
+                                            float pad_abs, float pad_rel) {
+    const int4 c = nodes[q].c;
+    float l[2][3], h[2][3];
+    const int refs[2] = {c.x, c.y};
+    for (int i = 0; i < 2; ++i) {
+        for (int a = 0; a < 3; ++a) {
+            l[i][a] = __int_as_float(0x7f800000);
+            h[i][a] = -__int_as_float(0x7f800000);
+        }
+        if (refs[i] >= 0) {
+            const float4 x = ldcg4(&nodes[refs[i]].x), y = ldcg4(&nodes[refs[i]].y), z = ldcg4(&nodes[refs[i]].z);
+            l[i][0] = fminf(x.x, x.z);
+            h[i][0] = fmaxf(x.y, x.w);
+            l[i][1] = fminf(y.x, y.z);
+            h[i][1] = fmaxf(y.y, y.w);
+            l[i][2] = fminf(z.x, z.z);
+            h[i][2] = fmaxf(z.y, z.w);
+        } else {
+            leaf_box(refs[i], recs, ftri, pad_abs, pad_rel, l[i], h[i]);
+        }
+    }
+    nodes[q].x = make_float4(l[0][0], h[0][0], l[1][0], h[1][0]);
+    nodes[q].y = make_float4(l[0][1], h[0][1], l[1][1], h[1][1]);
+    nodes[q].z = make_float4(l[0][2], h[0][2], l[1][2], h[1][2]);
+}
+
+__device__ __forceinline__ void refit4_node(Bvh4Node* nodes, int q, const TriHit* recs, const splat_ftri_t* ftri,
+                                            float pad_abs, float pad_rel) {
+    const int nc = nodes[q].meta.x;
+    const int4 c = nodes[q].c;
+    const int refs[4] = {c.x, c.y, c.z, c.w};
+    float lo[3][4], hi[3][4];
+    for (int i = 0; i < 4; ++i) {
+        float l[3] = {__int_as_float(0x7f800000), __int_as_float(0x7f800000), __int_as_float(0x7f800000)};
+        float h[3] = {-l[0], -l[0], -l[0]};
+        if (i < nc) {
+            if (refs[i] >= 0) {
+                const Bvh4Node* ch = nodes + refs[i];
+                const float4 lx = ldcg4(&ch->lox), hx = ldcg4(&ch->hix), ly = ldcg4(&ch->loy), hy = ldcg4(&ch->hiy);
+                const float4 lz = ldcg4(&ch->loz), hz = ldcg4(&ch->hiz);
+                const int cn = __ldcg(&ch->meta.x);
+                for (int j = 0; j < cn; ++j) {
+                    l[0] = fminf(l[0], comp(lx, j));
+                    h[0] = fmaxf(h[0], comp(hx, j));
+                    l[1] = fminf(l[1], comp(ly, j));
+                    h[1] = fmaxf(h[1], comp(hy, j));
+                    l[2] = fminf(l[2], comp(lz, j));
+                    h[2] = fmaxf(h[2], comp(hz, j));
                 }
-            }
-            for (int a = 0; a < 3; ++a) {
-                lo[a][i] = l[a];
-                hi[a][i] = h[a];
+            } else {
+                leaf_box(refs[i], recs, ftri, pad_abs, pad_rel, l, h);
             }
         }
-        nd.lox = make_float4(lo[0][0], lo[0][1], lo[0][2], lo[0][3]);
-        nd.hix = make_float4(hi[0][0], hi[0][1], hi[0][2], hi[0][3]);
-        nd.loy = make_float4(lo[1][0], lo[1][1], lo[1][2], lo[1][3]);
-        nd.hiy = make_float4(hi[1][0], hi[1][1], hi[1][2], hi[1][3]);
-        nd.loz = make_float4(lo[2][0], lo[2][1], lo[2][2], lo[2][3]);
-        nd.hiz = make_float4(hi[2][0], hi[2][1], hi[2][2], hi[2][3]);
+        for (int a = 0; a < 3; ++a) {
+            lo[a][i] = l[a];
+            hi[a][i] = h[a];
+        }
+    }
+    Bvh4Node& nd = nodes[q];
+    nd.lox = make_float4(lo[0][0], lo[0][1], lo[0][2], lo[0][3]);
+    nd.hix = make_float4(hi[0][0], hi[0][1], hi[0][2], hi[0][3]);
+    nd.loy = make_float4(lo[1][0], lo[1][1], lo[1][2], lo[1][3]);
+    nd.hiy = make_float4(hi[1][0], hi[1][1], hi[1][2], hi[1][3]);
+    nd.loz = make_float4(lo[2][0], lo[2][1], lo[2][2], lo[2][3]);
+    nd.hiz = make_float4(hi[2][0], hi[2][1], hi[2][2], hi[2][3]);
+}
+
+template <bool WIDE>
+__global__ void refit_tree_kernel(void* nodes_v, int64_t n_nodes, const int32_t* __restrict__ links, unsigned* flags,
+                                  const TriHit* __restrict__ recs, const splat_ftri_t* __restrict__ ftri,
+                                  float pad_abs, float pad_rel) {
+    for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q0 < n_nodes;
+         q0 += (int64_t)gridDim.x * blockDim.x) {
+        if (links[n_nodes + q0] != 0) continue;  // has inner children: reached by its last child
+        int q = (int)q0;
+        for (int64_t guard = 0; guard < n_nodes; ++guard) {
+            if (WIDE) refit4_node(reinterpret_cast<Bvh4Node*>(nodes_v), q, recs, ftri, pad_abs, pad_rel);
+            else refit2_node(reinterpret_cast<BvhNode*>(nodes_v), q, recs, ftri, pad_abs, pad_rel);
+            const int p = links[q];
+            if (p < 0) break;
+            __threadfence();
+            if ((int)atomicAdd(&flags[p], 1u) + 1 < links[n_nodes + p]) break;
+            __threadfence();
+            q = p;
+        }
     }
 }
 
-cudaError_t launch_refit4_level(Bvh4Node* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,
-                                const splat_ftri_t* ftri, float pad_abs, float pad_rel, cudaStream_t s) {
-    if (n_level <= 0) return cudaSuccess;
-    refit4_level_kernel<<<grid_for(n_level, 128, 152, 8), 128, 0, s>>>(nodes, level_nodes, n_level, bvh_recs, ftri,
-                                                                        pad_abs, pad_rel);
-    ++g_launches;
-    return cudaGetLastError();
-}
-
-cudaError_t launch_refit_level(BvhNode* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,
-                               const splat_ftri_t* ftri, float pad_abs, float pad_rel, cudaStream_t s) {
-    if (n_level <= 0) return cudaSuccess;
-    refit_level_kernel<<<grid_for(n_level, 128, 152, 8), 128, 0, s>>>(nodes, level_nodes, n_level, bvh_recs, ftri,
-                                                                       pad_abs, pad_rel);
+cudaError_t launch_refit_tree(void* nodes, bool wide, int64_t n_nodes, const int32_t* links, unsigned* flags,
+                              const TriHit* bvh_recs, const splat_ftri_t* ftri, float pad_abs, float pad_rel,
+                              cudaStream_t s) {
+    if (n_nodes <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(flags, 0, sizeof(unsigned) * (size_t)n_nodes, s);
+    if (e != cudaSuccess) return e;
+    if (wide)
+        refit_tree_kernel<true><<<grid_for(n_nodes, 128, 152, 8), 128, 0, s>>>(nodes, n_nodes, links, flags, bvh_recs,
+                                                                             ftri, pad_abs, pad_rel);
+    else
+        refit_tree_kernel<false><<<grid_for(n_nodes, 128, 152, 8), 128, 0, s>>>(nodes, n_nodes, links, flags, bvh_recs,
+                                                                              ftri, pad_abs, pad_rel);
     ++g_launches;
     return cudaGetLastError();
 }

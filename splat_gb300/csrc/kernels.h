@@ -76,8 +76,12 @@ cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh
                             int32_t* err, int sm_count, cudaStream_t s);
 // grid of a work-counter traversal launch (one resident wave)
 int resident_grid(const void* kernel, int64_t cap, int sm_count, int threads, int max_per_sm);
-cudaError_t launch_refit4_level(Bvh4Node* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,
-                                const splat_ftri_t* ftri, float pad_abs, float pad_rel, cudaStream_t s);
+// one-launch bottom-up refit of a two-child (wide = false) or four-wide tree;
+// links: parent per node, then number of inner children per node
+cudaError_t launch_refit_tree(void* nodes, bool wide, int64_t n_nodes, const int32_t* links, unsigned* flags,
+                              const TriHit* bvh_recs, const splat_ftri_t* ftri, float pad_abs, float pad_rel,
+                              cudaStream_t s);
+
 
 // GPU BVH rebuild (lbvh.cu): linear BVH over Morton-sorted centroids, written
 // as two-child and four-wide nodes with leaves of at most leaf_max triangles
@@ -89,8 +93,7 @@ cudaError_t launch_lbvh_build(const splat_ftri_t* ftri, int64_t n_tris, int leaf
 // scene packing / refit
 cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, const int32_t* bvh_order,
                              TriHit* bvh_recs, cudaStream_t s);
-cudaError_t launch_refit_level(BvhNode* nodes, const int32_t* level_nodes, int64_t n_level, const TriHit* bvh_recs,
-                               const splat_ftri_t* ftri, float pad_abs, float pad_rel, cudaStream_t s);
+
 
 // generation and conversion
 struct GenParams {
