@@ -187,23 +187,24 @@ __global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, 
 // One lane per queued ray, walking all of its planes: rays of one item are
 // adjacent in the queue, so a warp's lanes usually share an item and its
 // plane count, and no lane idles on frames with few planes.
-__global__ void __launch_bounds__(256, 3) batch_splat_kernel(RaySoA q, const int64_t* __restrict__ count,
+__global__ void __launch_bounds__(256, 2) batch_splat_kernel(RaySoA q, const int64_t* __restrict__ count,
                                                              const BatchItem* __restrict__ items) {
     const int64_t n = *count;
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
         const RayState r = load_ray(q, k);
         const BatchItem& it = items[q.id[k] >> kSlotShift];
-        const int planes = it.sp.n_lambda > 0 ? it.sp.n_lambda : 1;
+        const SplatView sp = splat_view(it.sp);
+        const int planes = sp.n_lambda > 0 ? sp.n_lambda : 1;
         const Tri T = load_tri(it.ftri, r.ignore);
         const TriUV quv = tri_uv(T);
-        for (int il = 0; il < planes; ++il) (void)splat_ray_plane(it.sp, r, T, quv, il);
+        for (int il = 0; il < planes; ++il) (void)splat_ray_plane(sp, r, T, quv, il);
     }
 }
 
 // The same through the block's shared texel table keyed by texel address
 // (rays of one block may splat into different items' maps): plane by plane
 // up to the block's largest plane count.
-__global__ void __launch_bounds__(256, 3) batch_splat_agg_kernel(RaySoA q, const int64_t* __restrict__ count,
+__global__ void __launch_bounds__(256, 2) batch_splat_agg_kernel(RaySoA q, const int64_t* __restrict__ count,
                                                                  const BatchItem* __restrict__ items) {
     __shared__ unsigned long long s_key[kAggSlots];
     __shared__ int32_t s_val[kAggSlots];

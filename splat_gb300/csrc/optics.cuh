@@ -408,7 +408,23 @@ __device__ __forceinline__ RayState gen_ray(const GenParams& g, int64_t kid) {
 // ---------------------------------------------------------------------------
 // light-map splat of one (ray, plane)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void flush_texel(const SplatParams& sp, int32_t off, int32_t vi, float vf) {
+// The scalars of a SplatParams held in registers, its arrays read in place
+// (the batch engine's per-item parameters live in global memory).
+struct SplatView {
+    void* map;
+    int32_t accum;
+    float scale;
+    int64_t w, h;
+    int32_t n_lambda, n_delta;
+    const float* spectrum;
+    const float* deltas;
+};
+__device__ __forceinline__ SplatView splat_view(const SplatParams& sp) {
+    return SplatView{sp.map, sp.accum, sp.scale, sp.w, sp.h, sp.n_lambda, sp.n_delta, sp.spectrum, sp.deltas};
+}
+
+template <class P>
+__device__ __forceinline__ void flush_texel(const P& sp, int32_t off, int32_t vi, float vf) {
     if (off < 0) return;
     if (sp.accum == SPLAT_ACCUM_I32)
         atomicAdd(reinterpret_cast<int*>(sp.map) + off, vi);
@@ -417,8 +433,9 @@ __device__ __forceinline__ void flush_texel(const SplatParams& sp, int32_t off, 
 }
 
 // Sends a texel's partial sum straight to the map.
+template <class P>
 struct DirectSink {
-    const SplatParams& sp;
+    const P& sp;
     __device__ __forceinline__ void operator()(int32_t off, int32_t vi, float vf) const { flush_texel(sp, off, vi, vf); }
 };
 
@@ -523,9 +540,9 @@ __device__ __forceinline__ void table_flush(const SplatParams& sp, int32_t* keys
 // The N x N sub-samples of one (ray, plane), x offset fastest; returns the
 // number of samples accumulated.  Consecutive samples on one texel are summed
 // in registers before they reach the sink.
-template <class Sink>
-__device__ __forceinline__ int splat_ray_plane(const SplatParams& sp, const RayState& r, const Tri& T,
-                                               const TriUV& quv, int il, const Sink& sink) {
+template <class P, class Sink>
+__device__ __forceinline__ int splat_ray_plane(const P& sp, const RayState& r, const Tri& T, const TriUV& quv, int il,
+                                               const Sink& sink) {
     const int nd = sp.n_delta;
     const int32_t W = (int32_t)sp.w, H = (int32_t)sp.h;
     const float Wf = (float)W, Hf = (float)H;
@@ -571,9 +588,9 @@ __device__ __forceinline__ int splat_ray_plane(const SplatParams& sp, const RayS
     return done;
 }
 
-__device__ __forceinline__ int splat_ray_plane(const SplatParams& sp, const RayState& r, const Tri& T,
-                                               const TriUV& quv, int il) {
-    return splat_ray_plane(sp, r, T, quv, il, DirectSink{sp});
+template <class P>
+__device__ __forceinline__ int splat_ray_plane(const P& sp, const RayState& r, const Tri& T, const TriUV& quv, int il) {
+    return splat_ray_plane(sp, r, T, quv, il, DirectSink<P>{sp});
 }
 
 }  // namespace splat
