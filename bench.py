@@ -325,6 +325,19 @@ def run_ours(args):
                 "peak_source": pk["source"], "algorithmic_bytes_per_launch": round(bytes_per_launch),
                 "avg_launch_ms": round(avg_launch_s * 1e3, 4),
                 "share": {k: round(v[1] / max(ms_all.value, 1e-12), 4) for k, v in prof_res.items()}}
+    if dom == "hit_brute":
+        # the brute-force hitter is FP32-issue bound: ray-triangle tests per
+        # second against the issue peak at ~35 FP32 ops per hoisted test
+        sm = C.c_int32()
+        name = C.create_string_buffer(128)
+        L.check(lib.splat_device_info(C.byref(sm), name, 128))
+        mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
+        tests = sum(sum(p) for p in per_step) * (wl.n_tris - 1)
+        tps = tests / (dom_ms / 1e3)
+        peak_tps = sm.value * 128 * mhz * 1e6 / 35.0
+        roofline["compute"] = {"bound": "fp32_issue", "tests_per_s": round(tps), "peak_tests_per_s": round(peak_tps),
+                               "frac": round(tps / peak_tps, 4), "ops_per_test": 35,
+                               "note": "peak = SMs x 128 lanes x max SM clock / 35 FP32 ops per test"}
 
     out = {
         "metric": "rays/s", "value": value, "unit": "rays/s", "n_gpus": world, "steps": K, "warmup": W,
