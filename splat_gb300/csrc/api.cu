@@ -162,6 +162,8 @@ struct splat_scene {
     int64_t n_tris = 0, first_diffuse = 0;
     splat_ftri_t* d_ftri = nullptr;
     TriHit* d_brute = nullptr;
+    TriBox* d_boxes = nullptr;   // padded boxes of the brute-force records
+    unsigned* d_scale = nullptr; // max |vertex coordinate| (float bits), sets the box padding
     int64_t n_recs = 0;
     BvhNode* d_nodes = nullptr;
     int64_t n_nodes = 0;
@@ -190,6 +192,8 @@ static void scene_free(splat_scene* s) {
     if (!s) return;
     cudaFree(s->d_ftri);
     cudaFree(s->d_brute);
+    cudaFree(s->d_boxes);
+    cudaFree(s->d_scale);
     cudaFree(s->d_nodes);
     cudaFree(s->d_bvh);
     cudaFree(s->d_order);
@@ -210,15 +214,16 @@ static cudaError_t dalloc(T** p, size_t bytes, int64_t& total) {
 
 static splat_status_t scene_pack(splat_scene* s, cudaStream_t st) {
     ProfScope ps(SPLAT_KERNEL_AUX, st);
-    cudaError_t e = launch_pack_hits(s->d_ftri, s->n_tris, s->d_brute, s->d_order, s->d_bvh, st);
+    cudaError_t e = launch_pack_hits(s->d_ftri, s->n_tris, s->d_brute, s->d_boxes, s->d_scale, s->d_order, s->d_bvh,
+                                     st);
     if (e != cudaSuccess) return cuda_fail(e, "pack hit records");
     if (s->d_nodes && s->d_links) {
-        e = launch_refit_tree(s->d_nodes, false, s->n_nodes, s->d_links, s->d_flags, s->d_bvh, s->d_ftri, s->pad_abs,
+        e = launch_refit_tree(s->d_nodes, false, s->n_nodes, s->d_links, s->d_flags, s->d_bvh, s->d_ftri, s->d_scale,
                               s->pad_rel, st);
         if (e != cudaSuccess) return cuda_fail(e, "BVH refit");
     }
     if (s->d_nodes4 && s->d_links4) {
-        e = launch_refit_tree(s->d_nodes4, true, s->n_nodes4, s->d_links4, s->d_flags, s->d_bvh, s->d_ftri, s->pad_abs,
+        e = launch_refit_tree(s->d_nodes4, true, s->n_nodes4, s->d_links4, s->d_flags, s->d_bvh, s->d_ftri, s->d_scale,
                               s->pad_rel, st);
         if (e != cudaSuccess) return cuda_fail(e, "BVH4 refit");
     }
@@ -282,6 +287,8 @@ splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris,
     };
     chk(dalloc(&s->d_ftri, sizeof(splat_ftri_t) * (size_t)n_tris, s->bytes));
     chk(dalloc(&s->d_brute, sizeof(TriHit) * (size_t)s->n_recs, s->bytes));
+    chk(dalloc(&s->d_boxes, sizeof(TriBox) * (size_t)s->n_recs, s->bytes));
+    chk(dalloc(&s->d_scale, sizeof(unsigned), s->bytes));
     chk(dalloc(&s->d_err, sizeof(int32_t) * 4, s->bytes));
     if (build_bvh_flag && !bvh.nodes.empty()) {
         s->n_nodes = (int64_t)bvh.nodes.size();
@@ -319,7 +326,8 @@ splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris,
         chk(cudaMemcpyAsync(s->d_links4, bvh.links4.data(), sizeof(int32_t) * bvh.links4.size(),
                             cudaMemcpyHostToDevice, st));
     }
-    if (e == cudaSuccess) chk(launch_pack_hits(s->d_ftri, n_tris, s->d_brute, s->d_order, s->d_bvh, st));
+    if (e == cudaSuccess)
+        chk(launch_pack_hits(s->d_ftri, n_tris, s->d_brute, s->d_boxes, s->d_scale, s->d_order, s->d_bvh, st));
     // host vectors above must outlive the async copies
     if (e == cudaSuccess) chk(cudaStreamSynchronize(st));
     if (e != cudaSuccess) {
@@ -391,7 +399,8 @@ static splat_status_t scene_rebuild_gpu(splat_scene* s, cudaStream_t st) {
     SPLAT_CUDA(launch_lbvh_build(s->d_ftri, s->n_tris, kLbvhLeaf, s->d_lbvh, s->d_nodes, s->d_nodes4, s->d_order,
                                  sm_count_current(), st),
                "scene_rebuild: build");
-    SPLAT_CUDA(launch_pack_hits(s->d_ftri, s->n_tris, s->d_brute, s->d_order, s->d_bvh, st), "scene_rebuild: pack");
+    SPLAT_CUDA(launch_pack_hits(s->d_ftri, s->n_tris, s->d_brute, s->d_boxes, s->d_scale, s->d_order, s->d_bvh, st),
+               "scene_rebuild: pack");
     s->gpu_bvh = true;
     s->n_nodes = need;
     s->n_nodes4 = need;
@@ -486,7 +495,8 @@ static splat_status_t hit_any(const splat_scene_t* s, int32_t hitter, const RayS
     if (bvh) {
         if (!s->d_nodes) {
             if (s->n_recs > 0) return fail(SPLAT_ERR_INVALID, "BVH hitter on a scene created without BVH");
-            e = launch_hit_brute(src, cap, s->d_brute, 0, hit_idx, hit_t, nullptr, s->d_err, sm_count_current(), st);
+            e = launch_hit_brute(src, cap, s->d_brute, s->d_boxes, 0, hit_idx, hit_t, nullptr, s->d_err,
+                                 sm_count_current(), st);
         } else if (hitter == SPLAT_HITTER_BVH) {
             e = launch_hit_bvh4(src, cap, Bvh4View{s->d_nodes4, s->d_bvh}, hit_idx, hit_t, s->d_err,
                                 sm_count_current(), st);
@@ -495,7 +505,8 @@ static splat_status_t hit_any(const splat_scene_t* s, int32_t hitter, const RayS
                                st);
         }
     } else if (hitter == SPLAT_HITTER_BRUTE) {
-        e = launch_hit_brute(src, cap, s->d_brute, s->n_recs, hit_idx, hit_t, tmp, s->d_err, sm_count_current(), st);
+        e = launch_hit_brute(src, cap, s->d_brute, s->d_boxes, s->n_recs, hit_idx, hit_t, tmp, s->d_err,
+                             sm_count_current(), st);
     } else {
         return fail(SPLAT_ERR_INVALID, "unknown hitter");
     }
@@ -1072,7 +1083,8 @@ splat_status_t splat_batch_admit(splat_batch_t* b, const splat_scene_t* scene, c
     g.seed = P->seed;
     g.light_index = 0;
     g.ray_begin = rb;
-    BatchSceneRef sc{scene->d_ftri, scene->d_brute, scene->d_nodes4, scene->d_bvh, scene->n_recs, scene->n_tris,
+    BatchSceneRef sc{scene->d_ftri, scene->d_brute, scene->d_boxes, scene->d_nodes4, scene->d_bvh, scene->n_recs,
+                     scene->n_tris,
                      scene->first_diffuse};
     const SplatParams sp =
         make_splat(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);

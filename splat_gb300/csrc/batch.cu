@@ -39,6 +39,7 @@ constexpr int kMaxBatchItems = 256;
 struct BatchItem {
     const splat_ftri_t* ftri;
     const TriHit* brute;
+    const TriBox* brute_boxes;
     const Bvh4Node* nodes4;
     const TriHit* bvh_tris;
     int64_t n_recs, n_tris, first_diffuse;
@@ -121,7 +122,7 @@ __global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t
         if (!ANY_BRUTE || (it.hitter == SPLAT_HITTER_BVH && it.nodes4))
             bvh4_closest(r, Bvh4View{it.nodes4, it.bvh_tris}, stack_ref, stack_t, err, best, bi);
         else
-            brute_closest(r, it.brute, it.n_recs, best, bi);
+            brute_closest(r, it.brute, it.brute_boxes, it.n_recs, best, bi);
         hit_idx[k] = bi;
     });
 }
@@ -289,6 +290,7 @@ void batch_fill_item(void* dst, const BatchSceneRef& sc, const GenParams& gen, i
     std::memset(&it, 0, sizeof(it));
     it.ftri = sc.ftri;
     it.brute = sc.brute;
+    it.brute_boxes = sc.brute_boxes;
     it.nodes4 = sc.nodes4;
     it.bvh_tris = sc.bvh_tris;
     it.n_recs = sc.n_recs;

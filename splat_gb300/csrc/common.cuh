@@ -119,6 +119,18 @@ struct __align__(16) TriHit {
 };
 static_assert(sizeof(TriHit) == 80, "TriHit layout");
 
+// Padded vertex box of a triangle (lo.xyz, hi.xyz; w unused): the box the
+// BVH's leaves use, pad = pad_abs + pad_rel |box diagonal|.  A ray that
+// misses it cannot be accepted by the triangle's test.
+struct __align__(16) TriBox {
+    float4 lo, hi;
+};
+static_assert(sizeof(TriBox) == 32, "TriBox layout");
+
+__host__ __device__ __forceinline__ float pad_abs_of_scale(float max_abs_coord) {
+    return 1.0e-4f * (max_abs_coord > 1.0f ? max_abs_coord : 1.0f);
+}
+
 __host__ __device__ __forceinline__ F3 f3(const float* p) { return {p[0], p[1], p[2]}; }
 
 // FTri as loaded into registers (src/geo.jl:18).

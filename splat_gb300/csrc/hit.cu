@@ -76,6 +76,7 @@ constexpr int kStages = 4;
 
 template <int RPT, bool AOS>
 __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, const TriHit* __restrict__ recs,
+                                                                  const TriBox* __restrict__ boxes,
                                                                   int64_t n_recs, int64_t per_split,
                                                                   int32_t* __restrict__ hit_idx,
                                                                   float* __restrict__ hit_t,
@@ -83,6 +84,7 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
                                                                   int32_t* err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TriHit* tiles = reinterpret_cast<TriHit*>(smem_raw);
+    TriBox* btiles = reinterpret_cast<TriBox*>(smem_raw + (size_t)kStages * kTile * sizeof(TriHit));
     __shared__ __align__(8) uint64_t bars[kStages];
 
     const int64_t n = src.d_count ? *src.d_count : src.n;
@@ -96,6 +98,7 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
     HitRay ray[RPT];
     float best[RPT];
     int32_t bi[RPT];
+    float inv[RPT][3], oinv[RPT][3];  // slab-test terms of the padded-box pre-test
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
         const int64_t k = ray0 + threadIdx.x + (int64_t)r * kBruteThreads;
@@ -106,6 +109,12 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
         }
         best[r] = __int_as_float(0x7f800000);
         bi[r] = 1;
+        inv[r][0] = safe_inv(ray[r].dx);
+        inv[r][1] = safe_inv(ray[r].dy);
+        inv[r][2] = safe_inv(ray[r].dz);
+        oinv[r][0] = ray[r].ox * inv[r][0];
+        oinv[r][1] = ray[r].oy * inv[r][1];
+        oinv[r][2] = ray[r].oz * inv[r][2];
     }
 
     if (threadIdx.x == 0) {
@@ -118,9 +127,10 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
         const int s = kt % kStages;
         const int64_t first = tb + (int64_t)kt * kTile;
         const uint32_t cnt = (uint32_t)min((int64_t)kTile, te - first);
-        const uint32_t bytes = cnt * (uint32_t)sizeof(TriHit);
-        mbar_arrive_expect_tx(&bars[s], bytes);
+        const uint32_t bytes = cnt * (uint32_t)sizeof(TriHit), bbytes = cnt * (uint32_t)sizeof(TriBox);
+        mbar_arrive_expect_tx(&bars[s], bytes + bbytes);
         bulk_g2s(tiles + s * kTile, recs + first, bytes, &bars[s]);
+        bulk_g2s(btiles + s * kTile, boxes + first, bbytes, &bars[s]);
     };
     if (threadIdx.x == 0) {
         for (int kt = 0; kt < min(kStages, n_tiles); ++kt) issue(kt);
@@ -138,11 +148,21 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
         }
         const int cnt = (int)min((int64_t)kTile, te - (tb + (int64_t)kt * kTile));
         const TriHit* tile = tiles + s * kTile;
+        const TriBox* btile = btiles + s * kTile;
 #pragma unroll 2
         for (int j = 0; j < cnt; ++j) {
-            const float4 q0 = tile[j].n_nv;
+            const float4 lo = btile[j].lo, hi = btile[j].hi;
 #pragma unroll
             for (int r = 0; r < RPT; ++r) {
+                // the padded box first (the BVH leaves' test): a ray that misses it
+                // cannot be accepted by the triangle's test
+                const float a0 = fmaf(lo.x, inv[r][0], -oinv[r][0]), b0 = fmaf(hi.x, inv[r][0], -oinv[r][0]);
+                const float a1 = fmaf(lo.y, inv[r][1], -oinv[r][1]), b1 = fmaf(hi.y, inv[r][1], -oinv[r][1]);
+                const float a2 = fmaf(lo.z, inv[r][2], -oinv[r][2]), b2 = fmaf(hi.z, inv[r][2], -oinv[r][2]);
+                const float tmin = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fminf(a2, b2));
+                const float tmax = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fmaxf(a2, b2));
+                if (!((tmin <= tmax) & (tmax >= 0.0f) & (tmin <= best[r]))) continue;
+                const float4 q0 = tile[j].n_nv;
                 float num, den;
                 if (!tri_candidate(q0, ray[r], best[r], num, den)) continue;
                 const float4 q1 = tile[j].a_idx;
@@ -227,8 +247,9 @@ cudaError_t launch_unpack_hits(const uint64_t* tmp, int64_t n, const int64_t* d_
 
 constexpr int kRPT = 2;
 
-cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs, int64_t n_recs, int32_t* hit_idx,
-                             float* hit_t, uint64_t* tmp, int32_t* err, int sm_count, cudaStream_t s) {
+cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs, const TriBox* boxes, int64_t n_recs,
+                             int32_t* hit_idx, float* hit_t, uint64_t* tmp, int32_t* err, int sm_count,
+                             cudaStream_t s) {
     if (cap <= 0) return cudaSuccess;
     const int64_t rays_per_block = (int64_t)kBruteThreads * kRPT;
     const int64_t ray_blocks = (cap + rays_per_block - 1) / rays_per_block;
@@ -243,7 +264,7 @@ cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs
     per_split = ((per_split + kTile - 1) / kTile) * kTile;
     splits = (n_recs + per_split - 1) / per_split;
     if (splits < 1) splits = 1;
-    const size_t smem = (size_t)kStages * kTile * sizeof(TriHit);
+    const size_t smem = (size_t)kStages * kTile * (sizeof(TriHit) + sizeof(TriBox));
     const bool use_tmp = splits > 1;
     if (use_tmp) {
         fill_u64_kernel<<<grid_for(cap, 256, sm_count, 8), 256, 0, s>>>((unsigned long long*)tmp, cap, rays.d_count,
@@ -254,10 +275,12 @@ cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs
     if (n_recs > 0) {
         if (rays.aos)
             hit_brute_kernel<kRPT, true><<<grid, kBruteThreads, smem, s>>>(
-                rays, recs, n_recs, per_split, hit_idx, hit_t, use_tmp ? (unsigned long long*)tmp : nullptr, err);
+                rays, recs, boxes, n_recs, per_split, hit_idx, hit_t, use_tmp ? (unsigned long long*)tmp : nullptr,
+                err);
         else
             hit_brute_kernel<kRPT, false><<<grid, kBruteThreads, smem, s>>>(
-                rays, recs, n_recs, per_split, hit_idx, hit_t, use_tmp ? (unsigned long long*)tmp : nullptr, err);
+                rays, recs, boxes, n_recs, per_split, hit_idx, hit_t, use_tmp ? (unsigned long long*)tmp : nullptr,
+                err);
         ++g_launches;
     } else {
         // no triangles: every ray misses
@@ -697,13 +720,47 @@ cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh
 // ---------------------------------------------------------------------------
 // scene packing and BVH refit
 // ---------------------------------------------------------------------------
-__global__ void pack_hits_kernel(const splat_ftri_t* __restrict__ ftri, int64_t n_tris, TriHit* brute,
-                                 const int32_t* __restrict__ bvh_order, TriHit* bvh) {
+// max |vertex coordinate| of the hit triangles (float bits; NaN skipped).
+__global__ void scene_scale_kernel(const splat_ftri_t* __restrict__ ftri, int64_t n_tris, unsigned* scale) {
+    unsigned m = 0u;
+    for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j + 1 < n_tris;
+         j += (int64_t)gridDim.x * blockDim.x) {
+        const float* p = ftri[j + 1].v[1];
+        for (int v = 0; v < 9; ++v) {
+            const float x = fabsf(p[v]);
+            if (x == x) m = max(m, __float_as_uint(x));
+        }
+    }
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(scale, m);
+}
+
+__device__ __forceinline__ void padded_box(const float* p, float pad_abs, float pad_rel, float lo[3], float hi[3]) {
+    float tl[3], th[3];
+    for (int a = 0; a < 3; ++a) {
+        tl[a] = fminf(fminf(p[a], p[3 + a]), p[6 + a]);
+        th[a] = fmaxf(fmaxf(p[a], p[3 + a]), p[6 + a]);
+    }
+    const float dx = th[0] - tl[0], dy = th[1] - tl[1], dz = th[2] - tl[2];
+    const float pad = pad_abs + pad_rel * sqrtf(dx * dx + dy * dy + dz * dz);
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = tl[a] - pad;
+        hi[a] = th[a] + pad;
+    }
+}
+
+__global__ void pack_hits_kernel(const splat_ftri_t* __restrict__ ftri, int64_t n_tris, TriHit* brute, TriBox* boxes,
+                                 const unsigned* __restrict__ scale, const int32_t* __restrict__ bvh_order,
+                                 TriHit* bvh) {
+    const float pad_abs = pad_abs_of_scale(__uint_as_float(*scale));
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j + 1 < n_tris;
          j += (int64_t)gridDim.x * blockDim.x) {
         // brute record j <- reference index j + 2 (the sentinel is never hit)
         const float* p = ftri[j + 1].v[0];
         brute[j] = pack_one((int32_t)(j + 2), f3(p), f3(p + 3), f3(p + 6), f3(p + 9));
+        float lo[3], hi[3];
+        padded_box(p + 3, pad_abs, 1.0e-3f, lo, hi);
+        boxes[j] = TriBox{make_float4(lo[0], lo[1], lo[2], 0.0f), make_float4(hi[0], hi[1], hi[2], 0.0f)};
         if (bvh) {
             const int32_t idx = bvh_order[j];
             const float* q = ftri[idx - 1].v[0];
@@ -712,11 +769,15 @@ __global__ void pack_hits_kernel(const splat_ftri_t* __restrict__ ftri, int64_t 
     }
 }
 
-cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, const int32_t* bvh_order,
-                             TriHit* bvh_recs, cudaStream_t s) {
+cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, TriBox* brute_boxes,
+                             unsigned* scale, const int32_t* bvh_order, TriHit* bvh_recs, cudaStream_t s) {
     if (n_tris <= 1) return cudaSuccess;
-    pack_hits_kernel<<<grid_for(n_tris, 256, 152, 8), 256, 0, s>>>(ftri, n_tris, brute_recs, bvh_order, bvh_recs);
-    ++g_launches;
+    cudaError_t e = cudaMemsetAsync(scale, 0, sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    scene_scale_kernel<<<grid_for(n_tris, 256, 152, 8), 256, 0, s>>>(ftri, n_tris, scale);
+    pack_hits_kernel<<<grid_for(n_tris, 256, 152, 8), 256, 0, s>>>(ftri, n_tris, brute_recs, brute_boxes, scale,
+                                                                    bvh_order, bvh_recs);
+    g_launches += 2;
     return cudaGetLastError();
 }
 
@@ -820,7 +881,8 @@ __device__ __forceinline__ void refit4_node(Bvh4Node* nodes, int q, const TriHit
 template <bool WIDE>
 __global__ void refit_tree_kernel(void* nodes_v, int64_t n_nodes, const int32_t* __restrict__ links, unsigned* flags,
                                   const TriHit* __restrict__ recs, const splat_ftri_t* __restrict__ ftri,
-                                  float pad_abs, float pad_rel) {
+                                  const unsigned* __restrict__ scale, float pad_rel) {
+    const float pad_abs = pad_abs_of_scale(__uint_as_float(*scale));
     for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q0 < n_nodes;
          q0 += (int64_t)gridDim.x * blockDim.x) {
         if (links[n_nodes + q0] != 0) continue;  // has inner children: reached by its last child
@@ -839,17 +901,17 @@ __global__ void refit_tree_kernel(void* nodes_v, int64_t n_nodes, const int32_t*
 }
 
 cudaError_t launch_refit_tree(void* nodes, bool wide, int64_t n_nodes, const int32_t* links, unsigned* flags,
-                              const TriHit* bvh_recs, const splat_ftri_t* ftri, float pad_abs, float pad_rel,
+                              const TriHit* bvh_recs, const splat_ftri_t* ftri, const unsigned* scale, float pad_rel,
                               cudaStream_t s) {
     if (n_nodes <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(flags, 0, sizeof(unsigned) * (size_t)n_nodes, s);
     if (e != cudaSuccess) return e;
     if (wide)
         refit_tree_kernel<true><<<grid_for(n_nodes, 128, 152, 8), 128, 0, s>>>(nodes, n_nodes, links, flags, bvh_recs,
-                                                                             ftri, pad_abs, pad_rel);
+                                                                             ftri, scale, pad_rel);
     else
         refit_tree_kernel<false><<<grid_for(n_nodes, 128, 152, 8), 128, 0, s>>>(nodes, n_nodes, links, flags, bvh_recs,
-                                                                              ftri, pad_abs, pad_rel);
+                                                                              ftri, scale, pad_rel);
     ++g_launches;
     return cudaGetLastError();
 }

@@ -298,12 +298,22 @@ __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid,
 }
 
 // Closest hit of one ray over hit records in reference-index order (the
-// per-ray form of the brute-force hitter; strict < keeps the smaller index).
-__device__ __forceinline__ void brute_closest(const HitRay& r, const TriHit* recs, int64_t n_recs, float& best_out,
-                                              int32_t& bi_out) {
+// per-ray form of the brute-force hitter; strict < keeps the smaller index),
+// each record behind its padded box as in the tiled kernel.
+__device__ __forceinline__ void brute_closest(const HitRay& r, const TriHit* recs, const TriBox* boxes,
+                                              int64_t n_recs, float& best_out, int32_t& bi_out) {
     float best = __int_as_float(0x7f800000);
     int32_t bi = 1;
+    const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
+    const float oix = r.ox * ix, oiy = r.oy * iy, oiz = r.oz * iz;
     for (int64_t j = 0; j < n_recs; ++j) {
+        const float4 lo = __ldg(&boxes[j].lo), hi = __ldg(&boxes[j].hi);
+        const float a0 = fmaf(lo.x, ix, -oix), b0 = fmaf(hi.x, ix, -oix);
+        const float a1 = fmaf(lo.y, iy, -oiy), b1 = fmaf(hi.y, iy, -oiy);
+        const float a2 = fmaf(lo.z, iz, -oiz), b2 = fmaf(hi.z, iz, -oiz);
+        const float tmin = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fminf(a2, b2));
+        const float tmax = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fmaxf(a2, b2));
+        if (!((tmin <= tmax) & (tmax >= 0.0f) & (tmin <= best))) continue;
         const TriHit* h = recs + j;
         float num, den;
         if (!tri_candidate(__ldg(&h->n_nv), r, best, num, den)) continue;

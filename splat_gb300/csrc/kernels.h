@@ -59,9 +59,11 @@ struct BvhView {
     const TriHit* tris;  // BVH order
 };
 
-// brute force over prepacked hit records (reference indices 2..T in order)
-cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs, int64_t n_recs, int32_t* hit_idx,
-                             float* hit_t, uint64_t* tmp, int32_t* err, int sm_count, cudaStream_t s);
+// brute force over prepacked hit records (reference indices 2..T in order),
+// each behind its padded box
+cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs, const TriBox* boxes, int64_t n_recs,
+                             int32_t* hit_idx, float* hit_t, uint64_t* tmp, int32_t* err, int sm_count,
+                             cudaStream_t s);
 // brute force over the reference's n_tris array (Tuple{Int32,Tri})
 cudaError_t launch_hit_brute_ntris(const splat_adray_t* rays, int64_t n_rays, const splat_ntri_t* ntris,
                                    int64_t n_tris, uint64_t* tmp, int32_t* hit_idx, int sm_count, cudaStream_t s);
@@ -79,7 +81,7 @@ int resident_grid(const void* kernel, int64_t cap, int sm_count, int threads, in
 // one-launch bottom-up refit of a two-child (wide = false) or four-wide tree;
 // links: parent per node, then number of inner children per node
 cudaError_t launch_refit_tree(void* nodes, bool wide, int64_t n_nodes, const int32_t* links, unsigned* flags,
-                              const TriHit* bvh_recs, const splat_ftri_t* ftri, float pad_abs, float pad_rel,
+                              const TriHit* bvh_recs, const splat_ftri_t* ftri, const unsigned* scale, float pad_rel,
                               cudaStream_t s);
 
 
@@ -90,9 +92,10 @@ size_t lbvh_scratch_bytes(int64_t n_prims);
 cudaError_t launch_lbvh_build(const splat_ftri_t* ftri, int64_t n_tris, int leaf_max, void* scratch,
                               BvhNode* nodes2, Bvh4Node* nodes4, int32_t* order, int sm_count, cudaStream_t s);
 
-// scene packing / refit
-cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, const int32_t* bvh_order,
-                             TriHit* bvh_recs, cudaStream_t s);
+// scene packing / refit.  scale: device word holding max |vertex coordinate|
+// (float bits), from which every padded box takes pad_abs = 1e-4 max(1, scale).
+cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, TriBox* brute_boxes,
+                             unsigned* scale, const int32_t* bvh_order, TriHit* bvh_recs, cudaStream_t s);
 
 
 // generation and conversion
@@ -200,6 +203,7 @@ cudaError_t launch_unpack_hits(const uint64_t* tmp, int64_t n, const int64_t* d_
 struct BatchSceneRef {
     const splat_ftri_t* ftri;
     const TriHit* brute;
+    const TriBox* brute_boxes;
     const Bvh4Node* nodes4;
     const TriHit* bvh_tris;
     int64_t n_recs, n_tris, first_diffuse;
