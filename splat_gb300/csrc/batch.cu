@@ -135,12 +135,19 @@ __global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, 
                                                                      const BatchItem* __restrict__ items, int tick,
                                                                      const int32_t* __restrict__ hit_idx,
                                                                      int32_t* err) {
-    __shared__ int s_keep[kBatchThreads / 32], s_dif[kBatchThreads / 32];
-    __shared__ unsigned long long s_kbase, s_dbase;
+    // double-buffered by iteration parity, as in evolve_kernel
+    __shared__ int s_keep2[2][kBatchThreads / 32], s_dif2[2][kBatchThreads / 32];
+    __shared__ unsigned long long s_kbase2[2], s_dbase2[2];
     const int64_t n = *in_count;
     const int lane = lane_id();
     const int wid = threadIdx.x >> 5;
-    for (int64_t base = (int64_t)blockIdx.x * kBatchThreads; base < n; base += (int64_t)gridDim.x * kBatchThreads) {
+    int par = 0;
+    for (int64_t base = (int64_t)blockIdx.x * kBatchThreads; base < n;
+         base += (int64_t)gridDim.x * kBatchThreads, par ^= 1) {
+        int* s_keep = s_keep2[par];
+        int* s_dif = s_dif2[par];
+        unsigned long long& s_kbase = s_kbase2[par];
+        unsigned long long& s_dbase = s_dbase2[par];
         const int64_t k = base + threadIdx.x;
         bool keep = false, dif = false;
         RayState o;
@@ -181,7 +188,6 @@ __global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, 
         const unsigned below = (1u << lane) - 1u;
         if (keep) store_ray(out, (int64_t)s_kbase + s_keep[wid] + __popc(kb & below), o, id);
         else if (dif) store_ray(queue, (int64_t)s_dbase + s_dif[wid] + __popc(db & below), o, id);
-        __syncthreads();
     }
 }
 

@@ -144,15 +144,26 @@ template <int MODE>
 __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
     constexpr bool TRACE = MODE != 0;
     constexpr bool SKY = MODE == 2;
-    __shared__ int s_warp[kEvolveThreads / 32];
-    __shared__ int s_wdif[kEvolveThreads / 32];
-    __shared__ int s_wsky[kEvolveThreads / 32];
-    __shared__ unsigned long long s_base, s_dbase, s_sbase;
+    // double-buffered by iteration parity: iteration i + 2 writes a buffer
+    // only after every thread has passed both barriers of iteration i + 1,
+    // so no third barrier is needed at the end of an iteration
+    __shared__ int s_warp2[2][kEvolveThreads / 32];
+    __shared__ int s_wdif2[2][kEvolveThreads / 32];
+    __shared__ int s_wsky2[2][kEvolveThreads / 32];
+    __shared__ unsigned long long s_base2[2], s_dbase2[2], s_sbase2[2];
     const int64_t n = *A.in_count;
     const int lane = lane_id();
     const int wid = threadIdx.x >> 5;
     const bool quirks = A.quirks != 0;
-    for (int64_t base = (int64_t)blockIdx.x * kEvolveThreads; base < n; base += (int64_t)gridDim.x * kEvolveThreads) {
+    int par = 0;
+    for (int64_t base = (int64_t)blockIdx.x * kEvolveThreads; base < n;
+         base += (int64_t)gridDim.x * kEvolveThreads, par ^= 1) {
+        int* s_warp = s_warp2[par];
+        int* s_wdif = s_wdif2[par];
+        int* s_wsky = s_wsky2[par];
+        unsigned long long& s_base = s_base2[par];
+        unsigned long long& s_dbase = s_dbase2[par];
+        unsigned long long& s_sbase = s_sbase2[par];
         const int64_t k = base + threadIdx.x;
         bool keep = false, dif = false, sky = false;
         RayState r, o;
@@ -209,7 +220,6 @@ __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
         } else if (SKY && sky) {
             store_ray(A.sky_q, (int64_t)s_sbase + s_wsky[wid] + __popc(sb & below), r, id);
         }
-        __syncthreads();
     }
 }
 
