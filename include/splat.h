@@ -180,6 +180,11 @@ splat_status_t splat_device_info(int32_t* sm_count, char* name, int32_t name_len
 splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris, int64_t first_diffuse,
                                   int32_t build_bvh, void* stream, splat_scene_t** out);
 splat_status_t splat_scene_destroy(splat_scene_t* scene);
+/* The scene's device error word, OR of the bits the plugin-level calls
+ * (next_hit, evolve, light map, shade) set on bad input -- 16: a hit index
+ * outside 1..n_tris, treated as a miss.  Synchronises the stream; with
+ * reset != 0 the word is cleared after the read. */
+splat_status_t splat_scene_errors(splat_scene_t* scene, int32_t reset, int32_t* out, void* stream);
 splat_status_t splat_scene_info(const splat_scene_t* scene, splat_scene_info_t* info);
 /* Device-side update from new FTri data of the same count (per-frame
  * geometry upload): repacks the hit records and refits the BVH boxes
@@ -256,6 +261,26 @@ splat_status_t splat_run_evolution(const splat_scene_t* scene, int32_t hitter, s
                                    int64_t n_rays, int32_t depth, const splat_material_t* material,
                                    float force_rand, uint64_t seed, uint32_t flags, int32_t* d_hit_idx,
                                    void* d_workspace, size_t workspace_bytes, void* stream);
+
+/* One evolve_ray broadcast (src/tracer.jl:181-201, as called at
+ * src/tracer.jl:246-256: `rays .= evolve_ray.(rays, hit_idx, tri_view, rndm,
+ * first_diffuse)`), in place.  Every ACTIVE ray k evolves with hit index
+ * d_hit_idx[k] (1-based) and Fresnel draw d_rndm[k] (the reference's rand!
+ * array); with d_rndm NULL the draw is force_rand when >= 0, else
+ * Philox(seed, (k, 0, 1, bounce)).  Rays that hit a diffuse triangle or
+ * nothing change only their status; retired rays are untouched. */
+splat_status_t splat_evolve(const splat_scene_t* scene, splat_adray_t* d_rays, int64_t n_rays,
+                            const int32_t* d_hit_idx, const float* d_rndm, const splat_material_t* material,
+                            float force_rand, uint64_t seed, uint32_t bounce, uint32_t flags, void* stream);
+
+/* partition!(rays, ray_swap; by = status != ACTIVE) (src/partition.jl:122-132,
+ * called at src/tracer.jl:263): the ACTIVE rays move to the front of d_rays,
+ * in no particular order (the reference's is not stable either), and their
+ * count is written to the device int64 *d_n_active -- it is not read back.
+ * Workspace: splat_partition_workspace_size(n_rays) bytes (the swap array). */
+size_t splat_partition_workspace_size(int64_t n_rays);
+splat_status_t splat_partition(splat_adray_t* d_rays, int64_t n_rays, int64_t* d_n_active, void* d_workspace,
+                               size_t workspace_bytes, void* stream);
 
 /* continuum_light_map2! (src/ray_imagers.jl:142-165): final_evolution of the
  * diffuse rays (in place) and the atomic spectrum splat into d_tex

@@ -98,6 +98,7 @@ SIGNATURES = {
     "splat_scene_info": ([vp, C.POINTER(SceneInfo)], i32),
     "splat_scene_update": ([vp, vp, vp], i32),
     "splat_scene_tris": ([vp], vp),
+    "splat_scene_errors": ([vp, i32, vp, vp], i32),
     "splat_scene_rebuild": ([vp, vp, vp], i32),
     "splat_rays_from_light": ([C.POINTER(RectLight), i64, C.POINTER(LambdaMode), u64, u32, vp, vp], i32),
     "splat_next_hit_brute": ([vp, i64, vp, i64, vp, vp, vp], i32),
@@ -105,6 +106,9 @@ SIGNATURES = {
     "splat_next_hit": ([vp, i32, vp, i64, vp, vp, vp], i32),
     "splat_run_evolution_workspace_size": ([i64], sz),
     "splat_run_evolution": ([vp, i32, vp, i64, i32, C.POINTER(Material), f32, u64, u32, vp, vp, sz, vp], i32),
+    "splat_evolve": ([vp, vp, i64, vp, vp, C.POINTER(Material), f32, u64, u32, u32, vp], i32),
+    "splat_partition_workspace_size": ([i64], sz),
+    "splat_partition": ([vp, i64, vp, vp, sz, vp], i32),
     "splat_continuum_light_map": ([vp, vp, i64, vp, vp, i32, i64, vp, i32, i32, i64, i64, vp], i32),
     "splat_trace_workspace_size": ([i64], sz),
     "splat_trace_forward": ([vp, C.POINTER(TraceParams), vp, vp, sz, vp, vp], i32),

@@ -362,6 +362,17 @@ splat_status_t splat_scene_info(const splat_scene_t* s, splat_scene_info_t* info
     return SPLAT_OK;
 }
 
+splat_status_t splat_scene_errors(splat_scene_t* s, int32_t reset, int32_t* out, void* stream) {
+    if (!s || !out) return fail(SPLAT_ERR_INVALID, "scene_errors: null argument");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    int32_t err = 0;
+    SPLAT_CUDA(cudaMemcpyAsync(&err, s->d_err, sizeof(err), cudaMemcpyDeviceToHost, st), "read error word");
+    SPLAT_CUDA(cudaStreamSynchronize(st), "read error word");
+    if (reset) SPLAT_CUDA(cudaMemsetAsync(s->d_err, 0, sizeof(int32_t), st), "clear error word");
+    *out = err;
+    return SPLAT_OK;
+}
+
 const splat_ftri_t* splat_scene_tris(const splat_scene_t* s) { return s ? s->d_ftri : nullptr; }
 
 // BVH of the scene's current FTri data rebuilt on the GPU (linear BVH).
@@ -624,6 +635,53 @@ splat_status_t splat_run_evolution(const splat_scene_t* scene, int32_t hitter, s
     all.aos = d_rays;
     all.n = n_rays;
     return hit_any(scene, hitter, all, n_rays, d_hit_idx, nullptr, w.tmp, st);
+}
+
+splat_status_t splat_evolve(const splat_scene_t* scene, splat_adray_t* d_rays, int64_t n_rays,
+                            const int32_t* d_hit_idx, const float* d_rndm, const splat_material_t* material,
+                            float force_rand, uint64_t seed, uint32_t bounce, uint32_t flags, void* stream) {
+    if (!scene || n_rays < 0) return fail(SPLAT_ERR_INVALID, "evolve: bad arguments");
+    if (!valid_material(material)) return fail(SPLAT_ERR_INVALID, "evolve: bad material");
+    if (n_rays == 0) return SPLAT_OK;
+    if (!d_rays || !d_hit_idx) return fail(SPLAT_ERR_INVALID, "evolve: null pointer");
+    EvolveArgs ea;
+    std::memset(&ea, 0, sizeof(ea));
+    ea.tris = scene->d_ftri;
+    ea.n_tris = scene->n_tris;
+    ea.err = scene->d_err;
+    ea.first_diffuse = scene->first_diffuse;
+    ea.material = *material;
+    ea.seed = seed;
+    ea.bounce = bounce;
+    ea.force_rand = force_rand;
+    ea.quirks = (flags & SPLAT_FLAG_REF_QUIRKS) ? 1 : 0;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    ProfScope ps(SPLAT_KERNEL_EVOLVE, st);
+    SPLAT_CUDA(launch_evolve_aos(d_rays, n_rays, d_hit_idx, d_rndm, ea, sm_count_current(), st), "evolve");
+    return SPLAT_OK;
+}
+
+static size_t partition_bytes(int64_t n_rays) {
+    return kAlign + (size_t)(n_rays > 0 ? n_rays : 0) * sizeof(splat_adray_t);
+}
+
+size_t splat_partition_workspace_size(int64_t n_rays) { return partition_bytes(n_rays); }
+
+splat_status_t splat_partition(splat_adray_t* d_rays, int64_t n_rays, int64_t* d_n_active, void* d_workspace,
+                               size_t workspace_bytes, void* stream) {
+    if (n_rays < 0 || !d_n_active || !d_workspace) return fail(SPLAT_ERR_INVALID, "partition: bad arguments");
+    if (n_rays > 0 && !d_rays) return fail(SPLAT_ERR_INVALID, "partition: null rays");
+    if (workspace_bytes < partition_bytes(n_rays)) return fail(SPLAT_ERR_WORKSPACE, "partition: workspace too small");
+    if (reinterpret_cast<uintptr_t>(d_workspace) % 16) return fail(SPLAT_ERR_INVALID, "partition: workspace not 16-byte aligned");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    int64_t* counts = reinterpret_cast<int64_t*>(d_workspace);
+    splat_adray_t* swap = reinterpret_cast<splat_adray_t*>(static_cast<char*>(d_workspace) + kAlign);
+    {
+        ProfScope ps(SPLAT_KERNEL_AUX, st);
+        SPLAT_CUDA(launch_partition(d_rays, n_rays, swap, counts, sm_count_current(), st), "partition");
+    }
+    SPLAT_CUDA(cudaMemcpyAsync(d_n_active, counts, sizeof(int64_t), cudaMemcpyDeviceToDevice, st), "partition count");
+    return SPLAT_OK;
 }
 
 splat_status_t splat_continuum_light_map(const splat_scene_t* scene, splat_adray_t* d_rays, int64_t n_rays,

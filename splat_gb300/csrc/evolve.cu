@@ -251,6 +251,85 @@ cudaError_t launch_evolve_plugin(const EvolveArgs& a, int64_t cap, int sm_count,
     return cudaGetLastError();
 }
 
+// evolve_ray broadcast (src/tracer.jl:181-201: `rays .= evolve_ray.(rays,
+// hit_idx, tri_view, rndm, first_diffuse)`) on the caller's AoS rays: every
+// ACTIVE ray evolves in place with its hit index and its Fresnel draw
+// rndm[k] (the reference's rand! output; without an array, Philox(seed) at
+// (k, 0, 1, bounce), or force_rand when >= 0); a ray that hits a diffuse
+// triangle or nothing only changes status; other rays are untouched.
+__global__ void __launch_bounds__(kEvolveThreads) evolve_aos_kernel(splat_adray_t* rays, int64_t n,
+                                                                    const int32_t* __restrict__ hit_idx,
+                                                                    const float* __restrict__ rndm, EvolveArgs A) {
+    const bool quirks = A.quirks != 0;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        splat_adray_t& a = rays[k];
+        if (a.status != kStatusActive) continue;
+        const RayState r = ray_from_aos(a);
+        const EvolveView v{A.tris, A.n_tris, A.err, A.first_diffuse, A.material, A.seed, A.bounce,
+                           rndm ? rndm[k] : A.force_rand, quirks, false};
+        RayState o;
+        int32_t ih;
+        const int fate = evolve_one<false>(r, hit_idx[k], (uint32_t)k, v, o, ih);
+        if (fate == kFateKeep) ray_to_aos(a, o, kStatusActive);
+        else if (fate == kFateDiffuse) a.status = (uint8_t)kStatusDiffuse;
+        else if (fate == kFateInfinity) a.status = (uint8_t)kStatusInfinity;
+    }
+}
+
+cudaError_t launch_evolve_aos(splat_adray_t* rays, int64_t n, const int32_t* hit_idx, const float* rndm,
+                              const EvolveArgs& a, int sm_count, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    evolve_aos_kernel<<<evolve_grid(n, sm_count), kEvolveThreads, 0, s>>>(rays, n, hit_idx, rndm, a);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+// partition! (src/partition.jl:10-132): the ACTIVE rays first, in no
+// particular order (the reference's blocks claim offsets atomically too).
+// counts[0] = number of ACTIVE rays (the result); counts[1], counts[2] =
+// active and other rays placed so far.
+__global__ void partition_count_kernel(const splat_adray_t* __restrict__ rays, int64_t n, int64_t* counts) {
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = base + threadIdx.x;
+        const unsigned m = __ballot_sync(kFull, k < n && rays[k].status == kStatusActive);
+        if (lane_id() == 0 && m) atomicAdd(reinterpret_cast<unsigned long long*>(&counts[0]), (unsigned long long)__popc(m));
+    }
+}
+
+__global__ void partition_scatter_kernel(const splat_adray_t* __restrict__ rays, int64_t n, int64_t* counts,
+                                         splat_adray_t* __restrict__ out) {
+    const int64_t n_active = counts[0];
+    unsigned long long* placed_active = reinterpret_cast<unsigned long long*>(&counts[1]);
+    unsigned long long* placed_other = reinterpret_cast<unsigned long long*>(&counts[2]);
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t k = base + threadIdx.x;
+        const bool valid = k < n;
+        const bool act = valid && rays[k].status == kStatusActive;
+        const unsigned ma = __ballot_sync(kFull, act), mi = __ballot_sync(kFull, valid && !act);
+        const unsigned below = (1u << lane_id()) - 1u;
+        unsigned long long ba = 0, bi = 0;
+        if (lane_id() == 0) {
+            if (ma) ba = atomicAdd(placed_active, (unsigned long long)__popc(ma));
+            if (mi) bi = atomicAdd(placed_other, (unsigned long long)__popc(mi));
+        }
+        ba = __shfl_sync(kFull, ba, 0);
+        bi = __shfl_sync(kFull, bi, 0);
+        if (act) out[(int64_t)ba + __popc(ma & below)] = rays[k];
+        else if (valid) out[n_active + (int64_t)bi + __popc(mi & below)] = rays[k];
+    }
+}
+
+cudaError_t launch_partition(splat_adray_t* rays, int64_t n, splat_adray_t* swap, int64_t* counts, int sm_count,
+                             cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(counts, 0, 3 * sizeof(int64_t), s);
+    if (e != cudaSuccess || n <= 0) return e;
+    partition_count_kernel<<<evolve_grid(n, sm_count), kEvolveThreads, 0, s>>>(rays, n, counts);
+    partition_scatter_kernel<<<evolve_grid(n, sm_count), kEvolveThreads, 0, s>>>(rays, n, counts, swap);
+    g_launches += 2;
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return cudaMemcpyAsync(rays, swap, sizeof(splat_adray_t) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+}
+
 // continuum_light_map2! on the caller's AoS rays: final_evolution in place,
 // then the splat.
 __global__ void __launch_bounds__(kEvolveThreads) light_map_kernel(splat_adray_t* rays, int64_t n,

@@ -153,6 +153,12 @@ cudaError_t launch_evolve_trace(const EvolveArgs& a, int64_t cap, int sm_count, 
 // trace mode plus the escaped rays queued for the skydome (camera pass)
 cudaError_t launch_evolve_camera(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s);
 cudaError_t launch_evolve_plugin(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s);
+// one evolve_ray broadcast on AoS rays (rndm: per-ray draws or null)
+cudaError_t launch_evolve_aos(splat_adray_t* rays, int64_t n, const int32_t* hit_idx, const float* rndm,
+                              const EvolveArgs& a, int sm_count, cudaStream_t s);
+// partition!: ACTIVE rays first via swap; counts[0] = their number (3 int64)
+cudaError_t launch_partition(splat_adray_t* rays, int64_t n, splat_adray_t* swap, int64_t* counts, int sm_count,
+                             cudaStream_t s);
 cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_idx, const splat_ftri_t* tris,
                              int64_t n_tris, int32_t* err, const SplatParams& sp, int sm_count, cudaStream_t s);
 // camera pass (shade.cu)

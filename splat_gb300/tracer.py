@@ -103,6 +103,12 @@ class Scene:
         """Per-frame geometry upload with the BVH rebuilt on the GPU."""
         L.check(L.load().splat_scene_rebuild(self.handle, _ptr(d_tris), _stream()))
 
+    def errors(self, reset: bool = True) -> int:
+        """The device error word (16: a hit index outside 1..n_tris); syncs."""
+        out = C.c_int32(0)
+        L.check(L.load().splat_scene_errors(self.handle, int(reset), C.byref(out), _stream()))
+        return int(out.value)
+
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
             L.load().splat_scene_destroy(self._h)
@@ -206,6 +212,33 @@ def run_evolution(hitter: int, scene: Scene, d_rays, depth: int, material, force
                                     int(seed), L.FLAG_REF_QUIRKS if quirks else 0, _ptr(hit), _ptr(workspace),
                                     workspace.numel(), _stream()))
     return hit
+
+
+def evolve(scene: Scene, d_rays, hit_idx, material, rndm=None, force_rand: Optional[float] = None, seed: int = 0,
+           bounce: int = 1, quirks: bool = True):
+    """One `rays .= evolve_ray.(rays, hit_idx, tri_view, rndm, first_diffuse)`
+    (src/tracer.jl:181-201, 246-256) in place; rndm is a device float32
+    array of per-ray Fresnel draws, or None for force_rand / Philox(seed)."""
+    n = n_rays_of(d_rays)
+    mat = _material(material)
+    fr = -1.0 if force_rand is None else float(force_rand)
+    L.check(L.load().splat_evolve(scene.handle, _ptr(d_rays), n, _ptr(hit_idx), _ptr(rndm), C.byref(mat), fr,
+                                  int(seed), int(bounce), L.FLAG_REF_QUIRKS if quirks else 0, _stream()))
+    return d_rays
+
+
+def partition(d_rays, workspace=None):
+    """partition!(rays, ray_swap; by = status != ACTIVE) (src/partition.jl:122-132):
+    ACTIVE rays to the front in place; returns the device int64 count."""
+    torch = _torch()
+    lib = L.load()
+    n = n_rays_of(d_rays)
+    need = int(lib.splat_partition_workspace_size(n))
+    if workspace is None or workspace.numel() < need:
+        workspace = torch.empty(need, dtype=torch.uint8, device="cuda")
+    count = torch.empty(1, dtype=torch.int64, device="cuda")
+    L.check(lib.splat_partition(_ptr(d_rays), n, _ptr(count), _ptr(workspace), workspace.numel(), _stream()))
+    return count
 
 
 def new_light_map(w: int, h: int, planes: int, accum: str = "f32"):
