@@ -19,7 +19,10 @@ the rays active in that bounce) per second of device time, whole job.
           splat_trace_forward_host sits beside it.
 * roofline: the kernel kind with the largest share of device time, its
           algorithmic bytes per launch over its event-timed launch duration,
-          against the measured HBM copy bandwidth.
+          against the measured HBM copy bandwidth.  Kernel times come from a
+          separate pass of steps with the splat overlap off, since in the
+          timed steps the splat of earlier bounces runs on a side stream
+          beside the later bounces.
 * cpu_baseline: the CPU restatement of the reference (oracle/, OpenMP over
           all host cores) on a bounded sample of the same workload.
 * --impl reference: that CPU implementation timed alone as the reference arm.
@@ -283,18 +286,42 @@ def run_ours(args):
     samples = int(st[:, 9].sum())
     errors = int(np.abs(st[:, 10]).sum())
 
+    n_all = C.c_int64()
+    L.check(lib.splat_profile_read(prof, L.KERNEL_ALL, C.byref(n_all), None))
+    lib.splat_profile_destroy(prof)
+
+    # Kernel times for the roofline come from a separate pass with the splat
+    # overlap off: in the timed steps the splat segments share the GPU with
+    # the later bounces, so per-kernel event times there overlap.
+    n_prof = min(K, 50)
+    old_overlap = int(lib.splat_get_tuning(L.TUNE_SPLAT_OVERLAP))
+    kprof = C.c_void_p()
+    L.check(lib.splat_profile_create(64 * (n_prof + 1), C.byref(kprof)))
+    kstats = torch.zeros((n_prof, 16), dtype=torch.int64, device="cuda")
+    L.check(lib.splat_set_tuning(L.TUNE_SPLAT_OVERLAP, 0))
+    try:
+        torch.cuda.synchronize()
+        L.check(lib.splat_profile_attach(kprof))
+        for i in range(n_prof):
+            flush.zero_()
+            run_step(W + K + i, kstats[i].data_ptr())
+        torch.cuda.synchronize()
+        L.check(lib.splat_profile_attach(None))
+    finally:
+        L.check(lib.splat_set_tuning(L.TUNE_SPLAT_OVERLAP, old_overlap))
     kinds = {"generate": L.KERNEL_GENERATE, "hit_brute": L.KERNEL_HIT_BRUTE, "hit_bvh": L.KERNEL_HIT_BVH,
              "evolve": L.KERNEL_EVOLVE, "splat": L.KERNEL_SPLAT, "aux": L.KERNEL_AUX}
     prof_res = {}
     for name, kd in kinds.items():
         n = C.c_int64()
         ms = C.c_double()
-        L.check(lib.splat_profile_read(prof, kd, C.byref(n), C.byref(ms)))
+        L.check(lib.splat_profile_read(kprof, kd, C.byref(n), C.byref(ms)))
         prof_res[name] = (int(n.value), float(ms.value))
-    n_all = C.c_int64()
     ms_all = C.c_double()
-    L.check(lib.splat_profile_read(prof, L.KERNEL_ALL, C.byref(n_all), C.byref(ms_all)))
-    lib.splat_profile_destroy(prof)
+    L.check(lib.splat_profile_read(kprof, L.KERNEL_ALL, None, C.byref(ms_all)))
+    lib.splat_profile_destroy(kprof)
+    kst = kstats.cpu().numpy()
+    kper_step = [[int(x) for x in kst[i, : wl.depth]] for i in range(n_prof)]
 
     if world > 1:
         import torch.distributed as dist
@@ -314,8 +341,9 @@ def run_ours(args):
     n_launch, dom_ms = prof_res[dom]
     launches_of_kind = {"hit_bvh": wl.depth, "hit_brute": wl.depth, "evolve": wl.depth, "splat": 1,
                         "generate": 1}[dom]
-    alg = sum(algorithmic_bytes(dom, wl, p, wl.n_tris, int(st[i, 8]), int(st[i, 9])) for i, p in enumerate(per_step))
-    n_kind_launches = K * launches_of_kind
+    alg = sum(algorithmic_bytes(dom, wl, p, wl.n_tris, int(kst[i, 8]), int(kst[i, 9]))
+              for i, p in enumerate(kper_step))
+    n_kind_launches = n_prof * launches_of_kind
     bytes_per_launch = alg / n_kind_launches
     avg_launch_s = dom_ms / 1e3 / n_kind_launches
     achieved = bytes_per_launch / avg_launch_s / 1e9
@@ -327,7 +355,8 @@ def run_ours(args):
                 "frac": round(achieved / pk["hbm_gbs"], 5), "traffic": traffic, "kernel": kernel_name,
                 "peak_source": pk["source"], "algorithmic_bytes_per_launch": round(bytes_per_launch),
                 "avg_launch_ms": round(avg_launch_s * 1e3, 4),
-                "share": {k: round(v[1] / max(ms_all.value, 1e-12), 4) for k, v in prof_res.items()}}
+                "share": {k: round(v[1] / max(ms_all.value, 1e-12), 4) for k, v in prof_res.items()},
+                "kernel_times": f"{n_prof} separate steps with the splat overlap off (L2 flushed between steps)"}
     if dom == "hit_brute":
         # the brute-force hitter is FP32-issue bound: ray-triangle tests per
         # second against the issue peak at ~35 FP32 ops per hoisted test
@@ -335,7 +364,7 @@ def run_ours(args):
         name = C.create_string_buffer(128)
         L.check(lib.splat_device_info(C.byref(sm), name, 128))
         mhz = (clocks or {}).get("sm_max_mhz") or 2070.0
-        tests = sum(sum(p) for p in per_step) * (wl.n_tris - 1)
+        tests = sum(sum(p) for p in kper_step) * (wl.n_tris - 1)
         tps = tests / (dom_ms / 1e3)
         peak_tps = sm.value * 128 * mhz * 1e6 / 35.0
         roofline["compute"] = {"bound": "fp32_issue", "tests_per_s": round(tps), "peak_tests_per_s": round(peak_tps),

@@ -461,7 +461,10 @@ enum {
     SPLAT_TUNE_BVH_PACKET = 5,           /* four-wide BVH warp packets: 0 never, 1 first bounce (default), 2 every bounce,
                                             3 / 4 first bounce + per-warp choice by ray spread after (loose /
                                             tight), 5 per-warp choice everywhere */
-    SPLAT_TUNE_KEYS = 6
+    SPLAT_TUNE_SPLAT_OVERLAP = 6,        /* fused trace step: 0 one splat after the last bounce; 1 the diffuse rays
+                                            of the earlier bounces splatted on a side stream while the last bounce
+                                            runs; 2 one splat per bounce on the side stream (default 2) */
+    SPLAT_TUNE_KEYS = 7
 };
 splat_status_t splat_set_tuning(int32_t key, int32_t value);
 int32_t splat_get_tuning(int32_t key);

@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <new>
 #include <string>
 #include <vector>
@@ -76,6 +77,7 @@ struct Work {
     int64_t* counts;  // counts[b] = active rays after bounce b (b <= 64); counts[kSplatCount] = queued
 };
 constexpr int kSplatCount = 96;
+constexpr int kSplatSnap = 100;  // counts[kSplatSnap + b]: splat queue length after bounce b (b <= 8)
 constexpr int kFetchBase = 128;  // counts[kFetchBase + b]: work counter of bounce b's hit launch (b <= 64)
 constexpr size_t kCounterBytes = 2048;
 
@@ -707,6 +709,31 @@ splat_status_t splat_continuum_light_map(const splat_scene_t* scene, splat_adray
 // ---------------------------------------------------------------------------
 size_t splat_trace_workspace_size(int64_t n_rays) { return n_rays <= 0 ? kAlign : work_bytes(n_rays); }
 
+// A side stream per (device, caller stream) of the calling host thread, with
+// fork / join events, for splats that run while later bounces trace.
+namespace {
+constexpr int kSideEvents = 10;
+struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev[kSideEvents] = {};
+};
+}  // namespace
+
+static cudaError_t side_stream_for(cudaStream_t caller, SideStream** out) {
+    thread_local std::map<std::pair<int, cudaStream_t>, SideStream> streams;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    SideStream& x = streams[{dev, caller}];
+    if (!x.s) {
+        if ((e = cudaStreamCreateWithFlags(&x.s, cudaStreamNonBlocking)) != cudaSuccess) return e;
+        for (cudaEvent_t& ev : x.ev)
+            if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return e;
+    }
+    *out = &x;
+    return cudaSuccess;
+}
+
 static int64_t grid_rays(const splat_trace_params_t* P) {
     return (P->light.res1 / P->upscale) * (P->light.res2 / P->upscale);
 }
@@ -767,6 +794,15 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
         make_splat(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
     ea.splat_q = w.q;
     ea.splat_count = &w.counts[kSplatCount];
+    // Splat overlap: the queue segment of bounces (seg, b] is splatted on the
+    // side stream from a snapshot of the queue length, while the main stream
+    // traces bounce b + 1.  Integer maps are sums, so the segmentation does
+    // not change them; float maps change only in summation order.
+    const int overlap = P->depth > 1 ? g_tune[SPLAT_TUNE_SPLAT_OVERLAP] : 0;
+    SideStream* side = nullptr;
+    if (overlap) SPLAT_CUDA(side_stream_for(st, &side), "side stream");
+    int64_t* snap = &w.counts[kSplatSnap];
+    int seg = 0, n_ev = 0;
     RaySoA cur = w.a, nxt = w.b;
     for (int32_t b = 1; b <= P->depth; ++b) {
         RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0,
@@ -785,10 +821,24 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
             SPLAT_CUDA(launch_evolve_trace(ea, cnt, sm, st), "evolve");
         }
         std::swap(cur, nxt);
+        if (overlap && b < P->depth && (overlap == 2 || b == P->depth - 1)) {
+            SPLAT_CUDA(launch_copy_count(&w.counts[kSplatCount], &snap[b], st), "queue snapshot");
+            SPLAT_CUDA(cudaEventRecord(side->ev[n_ev], st), "fork");
+            SPLAT_CUDA(cudaStreamWaitEvent(side->s, side->ev[n_ev++], 0), "fork");
+            ProfScope ps(SPLAT_KERNEL_SPLAT, side->s);
+            SPLAT_CUDA(launch_splat(w.q, &snap[seg], &snap[b], scene->d_ftri, sp, d_stats, sm, side->s), "splat");
+            seg = b;
+        }
     }
     {
         ProfScope ps(SPLAT_KERNEL_SPLAT, st);
-        SPLAT_CUDA(launch_splat(w.q, &w.counts[kSplatCount], scene->d_ftri, sp, d_stats, sm, st), "splat");
+        SPLAT_CUDA(launch_splat(w.q, seg ? &snap[seg] : nullptr, &w.counts[kSplatCount], scene->d_ftri, sp, d_stats,
+                                sm, st),
+                   "splat");
+    }
+    if (seg) {
+        SPLAT_CUDA(cudaEventRecord(side->ev[n_ev], side->s), "join");
+        SPLAT_CUDA(cudaStreamWaitEvent(st, side->ev[n_ev], 0), "join");
     }
     if (d_stats) {
         ProfScope ps(SPLAT_KERNEL_AUX, st);
@@ -839,6 +889,8 @@ splat_status_t splat_set_tuning(int32_t key, int32_t value) {
         if (value != 0 && value != 1) return fail(SPLAT_ERR_INVALID, "set_tuning: aggregate must be 0 or 1");
     } else if (key == SPLAT_TUNE_BVH_PACKET) {
         if (value < 0 || value > 5) return fail(SPLAT_ERR_INVALID, "set_tuning: packet mode must be 0..5");
+    } else if (key == SPLAT_TUNE_SPLAT_OVERLAP) {
+        if (value < 0 || value > 2) return fail(SPLAT_ERR_INVALID, "set_tuning: splat overlap must be 0..2");
     } else if (value < 1 || value > 256) {
         return fail(SPLAT_ERR_INVALID, "set_tuning: value must be 1..256");
     }

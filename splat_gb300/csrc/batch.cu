@@ -108,8 +108,7 @@ __global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t
                                                         const BatchItem* __restrict__ items, int32_t* hit_idx,
                                                         int32_t* err, unsigned long long* fetch) {
     const int64_t n = *count;
-    int stack_ref[kBvhStack];
-    float stack_t[kBvhStack];
+    int2 stack[kBvhStack];
     RaySrc src{};
     src.f = in.f;
     src.ignore = in.ignore;
@@ -120,7 +119,7 @@ __global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t
         float best;
         int32_t bi;
         if (!ANY_BRUTE || (it.hitter == SPLAT_HITTER_BVH && it.nodes4))
-            bvh4_closest(r, Bvh4View{it.nodes4, it.bvh_tris}, stack_ref, stack_t, err, best, bi);
+            bvh4_closest(r, Bvh4View{it.nodes4, it.bvh_tris}, stack, err, best, bi);
         else
             brute_closest(r, it.brute, it.brute_boxes, it.n_recs, best, bi);
         hit_idx[k] = bi;

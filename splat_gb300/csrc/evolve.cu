@@ -372,13 +372,16 @@ cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_
 // fastest; runs of samples on the same texel add in a register before one
 // atomic).  Integer maps are bit-exact; float maps change only the order of
 // additions, which float atomics never fix anyway.
-__global__ void __launch_bounds__(256, 2) splat_kernel(RaySoA q, const int64_t* __restrict__ d_count,
+__global__ void __launch_bounds__(256, 2) splat_kernel(RaySoA q, const int64_t* __restrict__ d_begin,
+                                                       const int64_t* __restrict__ d_count,
                                                        const splat_ftri_t* __restrict__ tris, SplatParams sp,
                                                        splat_trace_stats_t* st) {
+    const int64_t k0 = d_begin ? *d_begin : 0;
     const int64_t n = *d_count;
     const int planes = sp.n_lambda > 0 ? sp.n_lambda : 1;
     int done = 0;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t k = k0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
         const RayState r = load_ray(q, k);
         const Tri T = load_tri(tris, r.ignore);
         const TriUV quv = tri_uv(T);
@@ -390,17 +393,19 @@ __global__ void __launch_bounds__(256, 2) splat_kernel(RaySoA q, const int64_t* 
 // The same splat through the block's shared texel table: the block takes
 // 256 queued rays at a time and, plane by plane, sums their samples per
 // texel before one map atomic per distinct texel.
-__global__ void __launch_bounds__(256, 2) splat_agg_kernel(RaySoA q, const int64_t* __restrict__ d_count,
+__global__ void __launch_bounds__(256, 2) splat_agg_kernel(RaySoA q, const int64_t* __restrict__ d_begin,
+                                                           const int64_t* __restrict__ d_count,
                                                            const splat_ftri_t* __restrict__ tris, SplatParams sp,
                                                            splat_trace_stats_t* st) {
     __shared__ int32_t s_key[kAggSlots], s_val[kAggSlots];
+    const int64_t k0 = d_begin ? *d_begin : 0;
     const int64_t n = *d_count;
     const int planes = sp.n_lambda > 0 ? sp.n_lambda : 1;
     const TableSink sink{sp, s_key, s_val};
     table_clear(s_key, s_val);
     __syncthreads();
     int done = 0;
-    for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t base = k0 + (int64_t)blockIdx.x * blockDim.x; base < n; base += (int64_t)gridDim.x * blockDim.x) {
         const int64_t k = base + threadIdx.x;
         const bool live = k < n;
         RayState r;
@@ -421,16 +426,24 @@ __global__ void __launch_bounds__(256, 2) splat_agg_kernel(RaySoA q, const int64
     add_stats(st, 0, done);
 }
 
-cudaError_t launch_splat(const RaySoA& q, const int64_t* d_count, const splat_ftri_t* tris, const SplatParams& sp,
-                         splat_trace_stats_t* stats, int sm_count, cudaStream_t s) {
+cudaError_t launch_splat(const RaySoA& q, const int64_t* d_begin, const int64_t* d_count, const splat_ftri_t* tris,
+                         const SplatParams& sp, splat_trace_stats_t* stats, int sm_count, cudaStream_t s) {
     if (q.cap <= 0) return cudaSuccess;
     int64_t b = (q.cap + 255) / 256;
     const int64_t lim = (int64_t)sm_count * g_tune[SPLAT_TUNE_SPLAT_BLOCKS_PER_SM];
     if (b > lim) b = lim;
     if (g_tune[SPLAT_TUNE_SPLAT_AGGREGATE])
-        splat_agg_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_count, tris, sp, stats);
+        splat_agg_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_begin, d_count, tris, sp, stats);
     else
-        splat_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_count, tris, sp, stats);
+        splat_kernel<<<(int)(b < 1 ? 1 : b), 256, 0, s>>>(q, d_begin, d_count, tris, sp, stats);
+    ++g_launches;
+    return cudaGetLastError();
+}
+
+__global__ void copy_count_kernel(const int64_t* src, int64_t* dst) { *dst = *src; }
+
+cudaError_t launch_copy_count(const int64_t* src, int64_t* dst, cudaStream_t s) {
+    copy_count_kernel<<<1, 1, 0, s>>>(src, dst);
     ++g_launches;
     return cudaGetLastError();
 }

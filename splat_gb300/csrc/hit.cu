@@ -24,7 +24,7 @@
 namespace splat {
 
 thread_local int64_t g_launches = 0;
-int32_t g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1};
+int32_t g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1, 2};
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + bulk copy (sm_90+ async proxy)
@@ -464,8 +464,7 @@ template <bool AOS>
 __global__ void __launch_bounds__(kBvhThreads) hit_bvh_kernel(RaySrc src, BvhView bvh, int32_t* __restrict__ hit_idx,
                                                               float* __restrict__ hit_t, int32_t* err) {
     const int64_t n = src.d_count ? *src.d_count : src.n;
-    int stack_ref[kBvhStack];
-    float stack_t[kBvhStack];
+    int2 stack[kBvhStack];  // (ref, entry distance bits)
     for_each_ray(n, src.fetch, [&](int64_t k) {
         const HitRay r = load_hit_ray<AOS>(src, k);
         const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
@@ -502,9 +501,7 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh_kernel(RaySrc src, BvhVie
                         far_t = tmin0;
                     }
                     if (sp < kBvhStack) {
-                        stack_ref[sp] = far_ref;
-                        stack_t[sp] = far_t;
-                        ++sp;
+                        stack[sp++] = make_int2(far_ref, __float_as_int(far_t));
                     } else {
                         atomicOr(err, 2);
                     }
@@ -539,9 +536,9 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh_kernel(RaySrc src, BvhVie
             }
             bool found = false;
             while (sp > 0) {
-                --sp;
-                if (stack_t[sp] <= best) {
-                    ref = stack_ref[sp];
+                const int2 e = stack[--sp];
+                if (__int_as_float(e.y) <= best) {
+                    ref = e.x;
                     found = true;
                     break;
                 }
@@ -579,13 +576,12 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_kernel(RaySrc src, Bvh4V
                                                                int32_t* __restrict__ hit_idx,
                                                                float* __restrict__ hit_t, int32_t* err) {
     const int64_t n = src.d_count ? *src.d_count : src.n;
-    int stack_ref[kBvhStack];
-    float stack_t[kBvhStack];
+    int2 stack[kBvhStack];
     for_each_ray(n, src.fetch, [&](int64_t k) {
         const HitRay r = load_hit_ray<AOS>(src, k);
         float best;
         int32_t bi;
-        bvh4_closest(r, bvh, stack_ref, stack_t, err, best, bi);
+        bvh4_closest(r, bvh, stack, err, best, bi);
         hit_idx[k] = bi;
         if (hit_t) hit_t[k] = best;
     });
@@ -639,8 +635,7 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_packet_kernel(RaySrc src
         }
         extent = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
     }
-    int stack_ref[ADAPT ? kBvhStack : 1];
-    float stack_t[ADAPT ? kBvhStack : 1];
+    int2 lane_stack[ADAPT ? kBvhStack : 1];
     for_each_warp_batch(n, src.fetch, [&](int64_t base) {
         const int64_t k = base + lane;
         const bool valid = k < n;
@@ -655,7 +650,7 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_packet_kernel(RaySrc src
         if (packet) {
             bvh4_closest_packet(r, valid, bvh, stack, err, best, bi);
         } else if (ADAPT && valid) {
-            bvh4_closest(r, bvh, stack_ref, stack_t, err, best, bi);
+            bvh4_closest(r, bvh, lane_stack, err, best, bi);
         }
         if (valid) {
             hit_idx[k] = bi;

@@ -109,9 +109,10 @@ __device__ __forceinline__ float comp(const float4& v, int i) {
 // tests four child boxes; hit children are sorted by entry distance, the
 // nearest is visited next and the others are pushed farthest first with
 // their entry distance, so a popped entry beyond the current best hit is
-// skipped.  stack_ref / stack_t hold kBvhStack entries.
-__device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bvh, int* stack_ref, float* stack_t,
-                                             int32_t* err, float& best_out, int32_t& bi_out) {
+// skipped.  stack holds kBvhStack entries of (ref, entry distance bits), so
+// a push or a pop is one 8-byte local access.
+__device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bvh, int2* stack, int32_t* err,
+                                             float& best_out, int32_t& bi_out) {
     const float kInf = __int_as_float(0x7f800000);
     const float kMax = 3.402823466e38f;
     const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
@@ -148,18 +149,9 @@ __device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bv
             SPLAT_CSWAP(k1, r1, k2, r2);
             if (k0 < kInf) {
                 if (sp + 3 <= kBvhStack) {
-                    if (k3 < kInf) {
-                        stack_ref[sp] = r3;
-                        stack_t[sp++] = k3;
-                    }
-                    if (k2 < kInf) {
-                        stack_ref[sp] = r2;
-                        stack_t[sp++] = k2;
-                    }
-                    if (k1 < kInf) {
-                        stack_ref[sp] = r1;
-                        stack_t[sp++] = k1;
-                    }
+                    if (k3 < kInf) stack[sp++] = make_int2(r3, __float_as_int(k3));
+                    if (k2 < kInf) stack[sp++] = make_int2(r2, __float_as_int(k2));
+                    if (k1 < kInf) stack[sp++] = make_int2(r1, __float_as_int(k1));
                 } else {
                     atomicOr(err, 2);
                 }
@@ -186,9 +178,9 @@ __device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bv
         }
         bool found = false;
         while (sp > 0) {
-            --sp;
-            if (stack_t[sp] <= best) {
-                ref = stack_ref[sp];
+            const int2 e = stack[--sp];
+            if (__int_as_float(e.y) <= best) {
+                ref = e.x;
                 found = true;
                 break;
             }

@@ -195,9 +195,12 @@ cudaError_t launch_image_accumulate(float* out, const float* rgb, int64_t n, int
 cudaError_t launch_map_to_array(const int32_t* map, int64_t w, int64_t h, int64_t planes, float inv_scale,
                                 cudaSurfaceObject_t surf, int sm_count, cudaStream_t s);
 
-// light-map splat of the queued diffuse rays, one thread per (ray, sample)
-cudaError_t launch_splat(const RaySoA& q, const int64_t* d_count, const splat_ftri_t* tris, const SplatParams& sp,
-                         splat_trace_stats_t* stats, int sm_count, cudaStream_t s);
+// light-map splat of the queued diffuse rays [*d_begin, *d_count) (d_begin
+// null: from 0)
+cudaError_t launch_splat(const RaySoA& q, const int64_t* d_begin, const int64_t* d_count, const splat_ftri_t* tris,
+                         const SplatParams& sp, splat_trace_stats_t* stats, int sm_count, cudaStream_t s);
+// *dst = *src in stream order (a queue-length snapshot)
+cudaError_t launch_copy_count(const int64_t* src, int64_t* dst, cudaStream_t s);
 cudaError_t launch_stats_finish(const int64_t* counts, int depth, const int64_t* splat_count,
                                 splat_trace_stats_t* stats, const int32_t* err, cudaStream_t s);
 cudaError_t launch_unpack_hits(const uint64_t* tmp, int64_t n, const int64_t* d_count, int32_t* hit_idx,

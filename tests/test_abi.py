@@ -111,7 +111,7 @@ def test_tuning_knobs_validate_and_round_trip_without_gpu():
     """splat_set_tuning / splat_get_tuning are host-only: ranges are checked
     and values read back; unknown keys fail."""
     lib = L.load()
-    old = {k: lib.splat_get_tuning(k) for k in range(6)}
+    old = {k: lib.splat_get_tuning(k) for k in range(L.TUNE_KEYS)}
     try:
         assert old[L.TUNE_SPLAT_AGGREGATE] in (0, 1)
         assert lib.splat_set_tuning(L.TUNE_SPLAT_AGGREGATE, 2) == L.ERR_INVALID
@@ -123,8 +123,11 @@ def test_tuning_knobs_validate_and_round_trip_without_gpu():
         assert lib.splat_get_tuning(L.TUNE_BVH_BLOCKS_PER_SM) == 12
         assert lib.splat_set_tuning(L.TUNE_BVH_PACKET, 6) == L.ERR_INVALID
         assert lib.splat_set_tuning(L.TUNE_BVH_PACKET, 2) == L.OK
-        assert lib.splat_set_tuning(6, 1) == L.ERR_INVALID
-        assert lib.splat_get_tuning(6) == -1 and lib.splat_get_tuning(-1) == -1
+        assert lib.splat_set_tuning(L.TUNE_SPLAT_OVERLAP, 3) == L.ERR_INVALID
+        assert lib.splat_set_tuning(L.TUNE_SPLAT_OVERLAP, 2) == L.OK
+        assert lib.splat_get_tuning(L.TUNE_SPLAT_OVERLAP) == 2
+        assert lib.splat_set_tuning(L.TUNE_KEYS, 1) == L.ERR_INVALID
+        assert lib.splat_get_tuning(L.TUNE_KEYS) == -1 and lib.splat_get_tuning(-1) == -1
     finally:
         for k, v in old.items():
             L.check(lib.splat_set_tuning(k, v))
