@@ -372,7 +372,7 @@ cudaError_t launch_light_map(splat_adray_t* rays, int64_t n, const int32_t* hit_
 // fastest; runs of samples on the same texel add in a register before one
 // atomic).  Integer maps are bit-exact; float maps change only the order of
 // additions, which float atomics never fix anyway.
-__global__ void __launch_bounds__(256, 2) splat_kernel(RaySoA q, const int64_t* __restrict__ d_begin,
+__global__ void __launch_bounds__(256, 3) splat_kernel(RaySoA q, const int64_t* __restrict__ d_begin,
                                                        const int64_t* __restrict__ d_count,
                                                        const splat_ftri_t* __restrict__ tris, SplatParams sp,
                                                        splat_trace_stats_t* st) {

@@ -539,11 +539,13 @@ __device__ __forceinline__ void table_flush(const SplatParams& sp, int32_t* keys
 
 // The N x N sub-samples of one (ray, plane), x offset fastest; returns the
 // number of samples accumulated.  Consecutive samples on one texel are summed
-// in registers before they reach the sink.
-template <class P, class Sink>
-__device__ __forceinline__ int splat_ray_plane(const P& sp, const RayState& r, const Tri& T, const TriUV& quv, int il,
-                                               const Sink& sink) {
-    const int nd = sp.n_delta;
+// in registers before they reach the sink.  ND > 0: N known at compile time
+// (the sample loops unroll and the samples' arithmetic interleaves); 0: N =
+// sp.n_delta.
+template <int ND, class P, class Sink>
+__device__ __forceinline__ int splat_ray_plane_n(const P& sp, const RayState& r, const Tri& T, const TriUV& quv,
+                                                 int il, const Sink& sink) {
+    const int nd = ND > 0 ? ND : sp.n_delta;
     const int32_t W = (int32_t)sp.w, H = (int32_t)sp.h;
     const float Wf = (float)W, Hf = (float)H;
     int done = 0;
@@ -554,8 +556,10 @@ __device__ __forceinline__ int splat_ray_plane(const P& sp, const RayState& r, c
     const int32_t plane_off = il * W * H;
     int32_t run_off = -1, run_i = 0;
     float run_f = 0.f;
+#pragma unroll
     for (int iy = 0; iy < nd; ++iy) {
         const float dy = (r.y + sp.deltas[iy]) - r.y;
+#pragma unroll
         for (int ix = 0; ix < nd; ++ix) {
             const float dx = (r.x + sp.deltas[ix]) - r.x;
             const F3 pos = (pe + r.dpx * dx) + r.dpy * dy;
@@ -586,6 +590,14 @@ __device__ __forceinline__ int splat_ray_plane(const P& sp, const RayState& r, c
     }
     sink(run_off, run_i, run_f);
     return done;
+}
+
+template <class P, class Sink>
+__device__ __forceinline__ int splat_ray_plane(const P& sp, const RayState& r, const Tri& T, const TriUV& quv, int il,
+                                               const Sink& sink) {
+    if (sp.n_delta == 2) return splat_ray_plane_n<2>(sp, r, T, quv, il, sink);
+    if (sp.n_delta == 1) return splat_ray_plane_n<1>(sp, r, T, quv, il, sink);
+    return splat_ray_plane_n<0>(sp, r, T, quv, il, sink);
 }
 
 template <class P>
