@@ -14,8 +14,9 @@ the rays active in that bounce) per second of device time, whole job.
 * e2e:    the same step end to end through the C ABI with host buffers:
           every step uploads its pinned host triangles, repacks the scene and
           refits its BVH, traces, and downloads the light map to pinned host
-          memory, two frames in flight (the reference's real-time loop
-          double-buffers the same way); the one-frame-at-a-time figure through
+          memory, two frames in flight on two streams with two resident
+          scenes (the reference's real-time loop double-buffers the same
+          way); the one-frame-at-a-time figure through
           splat_trace_forward_host sits beside it.
 * roofline: the kernel kind with the largest share of device time, its
           algorithmic bytes per launch over its event-timed launch duration,
@@ -440,19 +441,24 @@ def e2e(step, wl, K, W, stream, world, rank):
 def e2e_pipelined(step, wl, K, W, stream, world, rank):
     """rays/s end to end with two frames in flight, the way the reference's
     real-time loop double-buffers its trace! calls (src/scenes/sphere.jl:
-    175-219): every step uploads its pinned host triangles, updates the scene
-    (repack + refit), traces into one of two light maps, and copies that map
-    and the step's counters to pinned host memory on a copy stream.  The copy
-    of step k overlaps step k + 1's upload and trace.  All through the C ABI
-    (splat_scene_update, splat_trace_forward) and cudaMemcpyAsync."""
+    175-219).  Frames alternate between two buffer sets, each with its own
+    compute stream, resident scene, workspace and light map.  Every step
+    uploads its pinned host triangles into its scene (splat_scene_update:
+    repack + refit), traces into its light map (splat_trace_forward), and
+    copies the map and the step's counters to pinned host memory on a copy
+    stream.  Step k + 1's upload and trace overlap step k's trace tail and
+    download.  All through the C ABI and cudaMemcpyAsync."""
     import torch
 
     from splat_gb300 import _lib as L
+    from splat_gb300 import tracer
 
     lib = L.load()
-    scene = step.scene
+    scenes = [step.scene, tracer.Scene(wl.tris, wl.first_diffuse, bvh=(wl.hitter != "brute"))]
+    streams = [stream, torch.cuda.Stream()]
+    wss = [step.ws, torch.empty_like(step.ws)]
     tris_pinned = torch.from_numpy(np.ascontiguousarray(wl.tris).reshape(-1)).pin_memory()
-    d_tris = torch.empty_like(tris_pinned, device="cuda")
+    d_tris = [torch.empty_like(tris_pinned, device="cuda") for _ in range(2)]
     maps = [step.tex, torch.empty_like(step.tex)]
     stats = [torch.zeros(16, dtype=torch.int64, device="cuda") for _ in range(2)]
     host_maps = [torch.empty(m.shape, dtype=m.dtype).pin_memory() for m in maps]
@@ -468,12 +474,14 @@ def e2e_pipelined(step, wl, K, W, stream, world, rank):
             copied[b].synchronize()  # step i - 2's map and counters are on the host: its buffers are free
             if i - 2 >= first_timed:
                 segs[0] += int(host_stats[b][:wl.depth].sum())
-        d_tris.copy_(tris_pinned, non_blocking=True)
-        scene.update(d_tris)
+        s = streams[b]
+        with torch.cuda.stream(s):
+            d_tris[b].copy_(tris_pinned, non_blocking=True)
+            scenes[b].update(d_tris[b])
         P.seed = wl.seed + 7 * i + 1000003 * rank
-        L.check(lib.splat_trace_forward(scene.handle, C.byref(P), maps[b].data_ptr(), step.ws.data_ptr(),
-                                        step.ws.numel(), stats[b].data_ptr(), stream.cuda_stream))
-        traced[b].record(stream)
+        L.check(lib.splat_trace_forward(scenes[b].handle, C.byref(P), maps[b].data_ptr(), wss[b].data_ptr(),
+                                        wss[b].numel(), stats[b].data_ptr(), s.cuda_stream))
+        traced[b].record(s)
         copy.wait_event(traced[b])
         with torch.cuda.stream(copy):
             host_maps[b].copy_(maps[b], non_blocking=True)
@@ -487,7 +495,9 @@ def e2e_pipelined(step, wl, K, W, stream, world, rank):
         torch.distributed.barrier()
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
-    t0.record(stream)
+    t0.record(copy)
+    for s in streams:
+        s.wait_event(t0)
     for i in range(K):
         one(W + i, (W + i) % 2, W)
     t1.record(copy)
@@ -497,6 +507,7 @@ def e2e_pipelined(step, wl, K, W, stream, world, rank):
             segs[0] += int(host_stats[j % 2][:wl.depth].sum())
     ms = t0.elapsed_time(t1)
     n_segs = segs[0]
+    scenes[1].close()
     if world > 1:
         import torch.distributed as dist
 
@@ -508,7 +519,8 @@ def e2e_pipelined(step, wl, K, W, stream, world, rank):
     return {"value": n_segs / (ms / 1e3), "unit": "rays/s", "h2d_bytes_per_step": int(wl.tris.nbytes),
             "d2h_bytes_per_step": int(step.tex.numel() * step.tex.element_size() + 8 * 16),
             "ms_per_step": ms / K,
-            "api": "pipelined, two frames in flight: splat_scene_update + splat_trace_forward + map/counter copies"}
+            "api": "two frames in flight on two streams and two resident scenes: splat_scene_update + "
+                   "splat_trace_forward + map/counter copies"}
 
 
 def run_reference(args):
