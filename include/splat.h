@@ -464,7 +464,9 @@ enum {
     SPLAT_TUNE_SPLAT_OVERLAP = 6,        /* fused trace step: 0 one splat after the last bounce; 1 the diffuse rays
                                             of the earlier bounces splatted on a side stream while the last bounce
                                             runs; 2 one splat per bounce on the side stream (default 2) */
-    SPLAT_TUNE_KEYS = 7
+    SPLAT_TUNE_BVH_REFILL = 7,           /* four-wide BVH, per-ray form: 0 a warp takes 32 new rays when all 32 are
+                                            done; 1..32 a warp refills its finished lanes once that many are done */
+    SPLAT_TUNE_KEYS = 8
 };
 splat_status_t splat_set_tuning(int32_t key, int32_t value);
 int32_t splat_get_tuning(int32_t key);

@@ -150,7 +150,8 @@ TUNE_SPLAT_BLOCKS_PER_SM = 3
 TUNE_SPLAT_AGGREGATE = 4
 TUNE_BVH_PACKET = 5
 TUNE_SPLAT_OVERLAP = 6
-TUNE_KEYS = 7
+TUNE_BVH_REFILL = 7
+TUNE_KEYS = 8
 
 KERNEL_GENERATE = 0
 KERNEL_HIT_BRUTE = 1

@@ -891,6 +891,8 @@ splat_status_t splat_set_tuning(int32_t key, int32_t value) {
         if (value < 0 || value > 5) return fail(SPLAT_ERR_INVALID, "set_tuning: packet mode must be 0..5");
     } else if (key == SPLAT_TUNE_SPLAT_OVERLAP) {
         if (value < 0 || value > 2) return fail(SPLAT_ERR_INVALID, "set_tuning: splat overlap must be 0..2");
+    } else if (key == SPLAT_TUNE_BVH_REFILL) {
+        if (value < 0 || value > 32) return fail(SPLAT_ERR_INVALID, "set_tuning: refill threshold must be 0..32");
     } else if (value < 1 || value > 256) {
         return fail(SPLAT_ERR_INVALID, "set_tuning: value must be 1..256");
     }

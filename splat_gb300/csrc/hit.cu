@@ -24,7 +24,7 @@
 namespace splat {
 
 thread_local int64_t g_launches = 0;
-int32_t g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1, 2};
+int32_t g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1, 2, 0};
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + bulk copy (sm_90+ async proxy)
@@ -588,6 +588,22 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_kernel(RaySrc src, Bvh4V
 }
 
 
+// The per-ray form with finished lanes refilled from the work counter.
+template <bool AOS>
+__global__ void __launch_bounds__(kBvhThreads) hit_bvh4_refill_kernel(RaySrc src, Bvh4View bvh,
+                                                                      int32_t* __restrict__ hit_idx,
+                                                                      float* __restrict__ hit_t, int32_t* err,
+                                                                      int refill_min) {
+    const int64_t n = src.d_count ? *src.d_count : src.n;
+    bvh4_refill_loop(
+        n, src.fetch, refill_min, err, [&](int64_t k) { return load_hit_ray<AOS>(src, k); },
+        [&](int64_t) { return bvh; },
+        [&](int64_t k, float best, int32_t bi) {
+            hit_idx[k] = bi;
+            if (hit_t) hit_t[k] = best;
+        });
+}
+
 // Spread of a warp's rays, max over axes of (max - min) of a coordinate.
 __device__ __forceinline__ float warp_spread(float a, float b, float c) {
     float m = 0.0f;
@@ -673,6 +689,8 @@ cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh
     if (!configured) {
         prefer_l1(hit_bvh4_kernel<true>);
         prefer_l1(hit_bvh4_kernel<false>);
+        prefer_l1(hit_bvh4_refill_kernel<true>);
+        prefer_l1(hit_bvh4_refill_kernel<false>);
         prefer_l1(hit_bvh_kernel<true>);
         prefer_l1(hit_bvh_kernel<false>);
         configured = true;
@@ -698,6 +716,17 @@ cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh
             else
                 hit_bvh4_packet_kernel<false, true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, ds, os);
         }
+        ++g_launches;
+        return cudaGetLastError();
+    }
+    if (rays.fetch && g_tune[SPLAT_TUNE_BVH_REFILL] > 0) {
+        const int grid = resident_grid(reinterpret_cast<const void*>(hit_bvh4_refill_kernel<false>), cap, sm_count,
+                                       kBvhThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
+        const int m = g_tune[SPLAT_TUNE_BVH_REFILL];
+        if (rays.aos)
+            hit_bvh4_refill_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, m);
+        else
+            hit_bvh4_refill_kernel<false><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, m);
         ++g_launches;
         return cudaGetLastError();
     }

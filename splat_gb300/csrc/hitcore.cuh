@@ -2,6 +2,8 @@
 // kernels (hit.cu) and the multi-scene batch kernels (batch.cu).
 #pragma once
 
+#include <climits>
+
 #include "kernels.h"
 
 namespace splat {
@@ -190,6 +192,133 @@ __device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bv
     best_out = best;
     bi_out = bi;
 }
+// Per-lane ray replacement over a work counter (the "dynamic fetch" of
+// Aila and Laine, "Understanding the efficiency of ray traversal on GPUs",
+// HPG 2009): every lane walks its own ray through the four-wide BVH exactly
+// as bvh4_closest does, one node or leaf per loop iteration, and when at
+// least refill_min lanes of the warp have finished, the warp takes that many
+// new rays from the counter in one atomic.  A warp no longer waits for its
+// slowest ray before the others start new work.  load(k) returns ray k,
+// view(k) the BVH it is traced in, store(k, t, index) takes its result.
+// Every node and leaf of a ray is entered at most once; kBvhVisitCap bounds
+// a ray's loop all the same (error bit 8).
+constexpr int kBvhVisitCap = 1 << 22;
+
+template <class Load, class View, class Store>
+__device__ __forceinline__ void bvh4_refill_loop(int64_t n, unsigned long long* fetch, int refill_min, int32_t* err,
+                                                 const Load& load, const View& view, const Store& store) {
+    constexpr int kDone = INT_MIN;  // no leaf reference is INT_MIN (at most 2^27 triangles)
+    const float kInf = __int_as_float(0x7f800000);
+    const float kMax = 3.402823466e38f;
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    int2 stack[kBvhStack];
+    HitRay r{};
+    Bvh4View bvh{};
+    float ix = 0.f, iy = 0.f, iz = 0.f, oix = 0.f, oiy = 0.f, oiz = 0.f, best = kInf;
+    int32_t bi = 1;
+    int sp = 0, node = kDone, visits = 0;
+    int64_t k = 0;
+    bool more = true;  // warp-uniform: the counter may still hold rays
+    while (true) {
+        const unsigned idle = __ballot_sync(0xffffffffu, node == kDone);
+        const int n_idle = __popc(idle);
+        if (more && (n_idle >= refill_min || idle == 0xffffffffu)) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(fetch, (unsigned long long)n_idle);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base + (unsigned long long)n_idle >= (unsigned long long)n) more = false;
+            if (node == kDone) {
+                const unsigned long long kk = base + (unsigned long long)__popc(idle & below);
+                if (kk < (unsigned long long)n) {
+                    k = (int64_t)kk;
+                    r = load(k);
+                    bvh = view(k);
+                    ix = safe_inv(r.dx);
+                    iy = safe_inv(r.dy);
+                    iz = safe_inv(r.dz);
+                    oix = r.ox * ix;
+                    oiy = r.oy * iy;
+                    oiz = r.oz * iz;
+                    best = kInf;
+                    bi = 1;
+                    sp = 0;
+                    node = 0;
+                    visits = 0;
+                }
+            }
+        }
+        if (!more && __all_sync(0xffffffffu, node == kDone)) break;
+        if (node == kDone) continue;
+        if (++visits > kBvhVisitCap) {
+            atomicOr(err, 8);
+            sp = 0;
+        } else if (node >= 0) {
+            const Bvh4Node* nd = bvh.nodes + node;
+            const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix);
+            const float4 ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
+            const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
+            const int4 c = __ldg(&nd->c);
+            const int nc = __ldg(&nd->meta.x);
+            float key[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float a0 = fmaf(comp(lx, i), ix, -oix), b0 = fmaf(comp(hx, i), ix, -oix);
+                const float a1 = fmaf(comp(ly, i), iy, -oiy), b1 = fmaf(comp(hy, i), iy, -oiy);
+                const float a2 = fmaf(comp(lz, i), iz, -oiz), b2 = fmaf(comp(hz, i), iz, -oiz);
+                const float tmin = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fminf(a2, b2));
+                const float tmax = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fmaxf(a2, b2));
+                const bool h = (i < nc) & (tmin <= tmax) & (tmax >= 0.0f) & (tmin <= best);
+                key[i] = h ? fminf(tmin, kMax) : kInf;
+            }
+            float k0 = key[0], k1 = key[1], k2 = key[2], k3 = key[3];
+            int r0 = c.x, r1 = c.y, r2 = c.z, r3 = c.w;
+            SPLAT_CSWAP(k0, r0, k1, r1);
+            SPLAT_CSWAP(k2, r2, k3, r3);
+            SPLAT_CSWAP(k0, r0, k2, r2);
+            SPLAT_CSWAP(k1, r1, k3, r3);
+            SPLAT_CSWAP(k1, r1, k2, r2);
+            if (k0 < kInf) {
+                if (sp + 3 <= kBvhStack) {
+                    if (k3 < kInf) stack[sp++] = make_int2(r3, __float_as_int(k3));
+                    if (k2 < kInf) stack[sp++] = make_int2(r2, __float_as_int(k2));
+                    if (k1 < kInf) stack[sp++] = make_int2(r1, __float_as_int(k1));
+                } else {
+                    atomicOr(err, 2);
+                }
+                node = r0;
+                continue;
+            }
+        } else {
+            const int enc = ~node;
+            const int first = enc >> 4;
+            const int count = (enc & 15) + 1;
+            for (int j = 0; j < count; ++j) {
+                const TriHit* h = bvh.tris + first + j;
+                float num, den;
+                if (!tri_candidate(__ldg(&h->n_nv), r, best, num, den)) continue;
+                const float4 q1 = __ldg(&h->a_idx);
+                const int32_t idx = __float_as_int(q1.w);
+                bool inside;
+                const float t = tri_t_from(num, den, q1, __ldg(&h->e0), __ldg(&h->e1), __ldg(&h->inv), r, inside);
+                if (inside & (t > 0.0f) & (idx != r.ig) & ((t < best) | ((t == best) & (idx < bi)))) {
+                    best = t;
+                    bi = idx;
+                }
+            }
+        }
+        node = kDone;
+        while (sp > 0) {
+            const int2 e = stack[--sp];
+            if (__int_as_float(e.y) <= best) {
+                node = e.x;
+                break;
+            }
+        }
+        if (node == kDone) store(k, best, bi);
+    }
+}
+
 #undef SPLAT_CSWAP
 
 // Packet traversal of a four-wide BVH: the 32 rays of a warp walk one

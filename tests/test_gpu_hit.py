@@ -4,7 +4,7 @@ bit-identical; BVH must equal brute force bit for bit."""
 import numpy as np
 import pytest
 
-from helpers import random_rays, small_scene
+from helpers import assert_rays_equal, random_rays, small_scene
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
@@ -200,3 +200,37 @@ def test_packet_traversal_matches_oracle(torch_cuda):
         assert np.array_equal(hit, o_hit)
     finally:
         L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, old))
+
+
+def test_refill_traversal_matches_oracle(torch_cuda):
+    """The per-ray four-wide traversal with finished lanes refilled from the
+    work counter (SPLAT_TUNE_BVH_REFILL) at several thresholds: run_evolution!
+    bit for bit against the oracle, and the fused step's map identical to the
+    one without refills."""
+    from splat_gb300 import _lib as L
+    from splat_gb300 import scenes as S
+    from splat_gb300 import tracer
+    from splat_gb300 import types as T
+
+    lib = L.load()
+    old = lib.splat_get_tuning(L.TUNE_BVH_REFILL)
+    tris, fd = small_scene(3, 0.05)
+    scene = tracer.Scene(tris, fd, bvh=True)
+    rays = O.rays_from_light(S.hemisphere_light(1, 48, 1.05), 1, (T.LAMBDA_UNIFORM, 1, 400.0, 700.0), seed=9)
+    ref, ref_hit = O.run_evolution(rays, tris, 4, fd, S.CAUCHY_GLASS, None, seed=3)
+    wl = S.realtime(light=S.scaled_light(S.realtime().light, 384))
+    sc = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
+    try:
+        L.check(lib.splat_set_tuning(L.TUNE_BVH_REFILL, 0))
+        base = tracer.trace_forward(wl, scene=sc).tex.cpu().numpy()
+        for m in (1, 7, 32):
+            L.check(lib.splat_set_tuning(L.TUNE_BVH_REFILL, m))
+            d = tracer.rays_to_device(rays)
+            hit = tracer.run_evolution(tracer.BVH, scene, d, 4, S.CAUCHY_GLASS, None, seed=3)
+            assert_rays_equal(tracer.rays_to_host(d), ref, f"refill {m}")
+            assert np.array_equal(hit.cpu().numpy(), ref_hit)
+            got = tracer.trace_forward(wl, scene=sc).tex.cpu().numpy()
+            assert np.array_equal(got, base) and base.sum() > 0
+    finally:
+        L.check(lib.splat_set_tuning(L.TUNE_BVH_REFILL, old))
+    assert scene.errors() == 0 and sc.errors() == 0
