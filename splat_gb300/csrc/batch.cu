@@ -64,24 +64,51 @@ struct FreshList {
     int64_t offset[kMaxBatchItems];
 };
 
-__global__ void batch_reserve_kernel(const BatchItem* items, int n_slots, int tick, int64_t* cur_count,
-                                     FreshList* fresh) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    int f = 0;
-    int64_t run = 0;
+// The items starting this tick, in slot order, get consecutive pool ranges
+// after the survivors: one thread per slot, block-wide exclusive scans of
+// (starts, rays).
+__global__ void __launch_bounds__(kMaxBatchItems) batch_reserve_kernel(const BatchItem* items, int n_slots, int tick,
+                                                                       int64_t* cur_count, FreshList* fresh) {
+    __shared__ int s_wcount[kMaxBatchItems / 32];
+    __shared__ long long s_wrays[kMaxBatchItems / 32];
+    const int s = threadIdx.x;
+    const int lane = s & 31, wid = s >> 5;
+    const bool starts = s < n_slots && items[s].start_tick == tick;
+    const long long nr = starts ? (long long)items[s].n_rays : 0;
+    const unsigned m = __ballot_sync(0xffffffffu, starts);
+    long long incl = nr;  // inclusive scan of the rays within the warp
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) {
+        s_wcount[wid] = __popc(m);
+        s_wrays[wid] = incl;
+    }
     const int64_t base = *cur_count;
-    for (int s = 0; s < n_slots; ++s) {
-        if (items[s].start_tick != tick) continue;
+    __syncthreads();
+    int cbase = 0;
+    long long rbase = 0;
+    for (int w = 0; w < wid; ++w) {
+        cbase += s_wcount[w];
+        rbase += s_wrays[w];
+    }
+    if (starts) {
+        const int f = cbase + __popc(m & ((1u << lane) - 1u));
+        const long long run = rbase + incl - nr;
         fresh->slot[f] = s;
         fresh->prefix[f] = run;
         fresh->offset[f] = base + run;
-        run += items[s].n_rays;
-        ++f;
     }
-    fresh->prefix[f] = run;
-    fresh->n = f;
-    fresh->total = run;
-    *cur_count = base + run;
+    __syncthreads();  // every thread has read *cur_count
+    if (s == kMaxBatchItems - 1) {
+        const int n_fresh = cbase + __popc(m);
+        const long long total = rbase + incl;
+        fresh->prefix[n_fresh] = total;
+        fresh->n = n_fresh;
+        fresh->total = total;
+        *cur_count = base + total;
+    }
 }
 
 __global__ void batch_generate_kernel(const BatchItem* __restrict__ items, const FreshList* __restrict__ fresh,
@@ -256,7 +283,7 @@ static int grid_cap(int64_t n, int threads, int sm_count, int per_sm) {
 cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s) {
     const BatchItem* items = reinterpret_cast<const BatchItem*>(a.items);
     FreshList* fresh = reinterpret_cast<FreshList*>(a.fresh);
-    batch_reserve_kernel<<<1, 32, 0, s>>>(items, a.n_slots, a.tick, a.cur_count, fresh);
+    batch_reserve_kernel<<<1, kMaxBatchItems, 0, s>>>(items, a.n_slots, a.tick, a.cur_count, fresh);
     ++g_launches;
     if (a.fresh_rays > 0) {
         batch_generate_kernel<<<grid_cap(a.fresh_rays, 256, a.sm_count, 8), 256, 0, s>>>(items, fresh, a.cur);
