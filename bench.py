@@ -876,7 +876,8 @@ def run_render(args):
            "clocks": clocks,
            "e2e": {"value": 1.0 / e2e_s, "unit": "frames/s", "ms_per_step": e2e_s * 1e3,
                    "h2d_bytes_per_step": int(host_tris.numel() * 4), "d2h_bytes_per_step": int(host_img.numel() * 4),
-                   "api": "scene_update + trace_forward + shader_set_light_map + render_camera + image_accumulate"},
+                   "api": "scene_update + trace_forward + shader_set_light_map + render_camera_after (camera "
+                          "bounces on a second stream, shading after the map) + image_accumulate"},
            "cpu_baseline": cpu}
     print(json.dumps(out), flush=True)
 

@@ -404,6 +404,14 @@ size_t splat_render_workspace_size(int64_t n_camera_rays);
 splat_status_t splat_render_camera(const splat_scene_t* scene, const splat_shader_t* shader,
                                    const splat_render_params_t* params, float* d_rgb, void* d_workspace,
                                    size_t workspace_bytes, void* stream);
+/* The same, with the shading held back until map_ready (a cudaEvent_t, e.g.
+ * recorded after splat_shader_set_light_map on another stream) has
+ * completed.  The camera rays' bounce loop does not read the light map, so
+ * on its own stream it runs while the frame's forward step is still
+ * tracing.  map_ready NULL: as splat_render_camera. */
+splat_status_t splat_render_camera_after(const splat_scene_t* scene, const splat_shader_t* shader,
+                                         const splat_render_params_t* params, float* d_rgb, void* d_workspace,
+                                         size_t workspace_bytes, void* stream, void* map_ready);
 
 /* Running average of a frame's iterations (src/tracer.jl:380-384):
  * iteration k = 1 copies rgb into out; k > 1 sets

@@ -124,6 +124,7 @@ SIGNATURES = {
     "splat_continuum_shade": ([vp, vp, vp, i64, vp, vp, vp, i32, i64, i64, i64, vp, vp], i32),
     "splat_render_workspace_size": ([i64], sz),
     "splat_render_camera": ([vp, vp, C.POINTER(RenderParams), vp, vp, sz, vp], i32),
+    "splat_render_camera_after": ([vp, vp, C.POINTER(RenderParams), vp, vp, sz, vp, vp], i32),
     "splat_image_accumulate": ([vp, vp, i64, i32, vp], i32),
     "splat_batch_device_bytes": ([i32, i64], sz),
     "splat_batch_create": ([i32, i64, vp], i32),

@@ -1641,6 +1641,12 @@ size_t splat_render_workspace_size(int64_t n_camera_rays) {
 splat_status_t splat_render_camera(const splat_scene_t* scene, const splat_shader_t* shader,
                                    const splat_render_params_t* P, float* d_rgb, void* d_workspace,
                                    size_t workspace_bytes, void* stream) {
+    return splat_render_camera_after(scene, shader, P, d_rgb, d_workspace, workspace_bytes, stream, nullptr);
+}
+
+splat_status_t splat_render_camera_after(const splat_scene_t* scene, const splat_shader_t* shader,
+                                         const splat_render_params_t* P, float* d_rgb, void* d_workspace,
+                                         size_t workspace_bytes, void* stream, void* map_ready) {
     if (!scene || !shader || !P) return fail(SPLAT_ERR_INVALID, "render_camera: null argument");
     if (!camera_ok(&P->camera)) return fail(SPLAT_ERR_INVALID, "render_camera: bad camera");
     splat_status_t rc = check_image(P->height, P->width, P->upscale);
@@ -1706,6 +1712,7 @@ splat_status_t splat_render_camera(const splat_scene_t* scene, const splat_shade
     }
     const ShadeParams sp =
         shade_params(shader, P->spectrum, &P->retina[0][0], P->n_lambda, P->upscale, P->height, d_rgb, SPLAT_MAX_LAMBDA);
+    if (map_ready) SPLAT_CUDA(cudaStreamWaitEvent(st, reinterpret_cast<cudaEvent_t>(map_ready), 0), "wait for the map");
     ProfScope ps(SPLAT_KERNEL_SHADE, st);
     SPLAT_CUDA(launch_shade_queues(w.q, &w.counts[kSplatCount], sky, sky_count, scene->d_ftri, sp, cnt, sm, st),
                "shade");

@@ -477,10 +477,17 @@ class CameraPass:
         self.ws = torch.empty(int(L.load().splat_render_workspace_size(n)), dtype=torch.uint8, device="cuda")
         self.rgb = new_image(params.height, params.width)
 
-    def run(self, stream: Optional[int] = None):
-        L.check(L.load().splat_render_camera(self.scene.handle, self.shader.handle, C.byref(self.params),
-                                             _ptr(self.rgb), _ptr(self.ws), self.ws.numel(),
-                                             _stream() if stream is None else stream))
+    def run(self, stream: Optional[int] = None, map_ready=None):
+        """Enqueue the pass; with map_ready (a torch.cuda.Event) the shading
+        waits for it while the camera rays' bounce loop does not."""
+        st = _stream() if stream is None else stream
+        if map_ready is None:
+            L.check(L.load().splat_render_camera(self.scene.handle, self.shader.handle, C.byref(self.params),
+                                                 _ptr(self.rgb), _ptr(self.ws), self.ws.numel(), st))
+        else:
+            L.check(L.load().splat_render_camera_after(self.scene.handle, self.shader.handle, C.byref(self.params),
+                                                       _ptr(self.rgb), _ptr(self.ws), self.ws.numel(), st,
+                                                       map_ready.cuda_event))
         return self.rgb
 
 
@@ -548,11 +555,28 @@ class Renderer:
         return self.step.tex
 
     def run(self):
+        """Enqueue the frame on the current stream.  The camera pass runs on a
+        second stream: its bounce loop overlaps the forward step, and its
+        shading waits for the light map; the current stream waits for the
+        image at the end, so the frame is ordered like a one-stream call."""
         lib = L.load()
+        torch = self._torch
+        main = torch.cuda.current_stream()
+        if not hasattr(self, "_cam_stream"):
+            self._cam_stream = torch.cuda.Stream()
+            self._map_ready = torch.cuda.Event()
+            self._shaded = torch.cuda.Event()
+        cam = self._cam_stream
+        cam.wait_stream(main)  # inputs enqueued before the frame (geometry, base map) are in place
         for k in range(1, self.iterations + 1):
             self.forward(k)
+            if k > 1:
+                main.wait_event(self._shaded)  # the previous iteration's shading has read the texture
             self.shader.set_light_map(self.step.tex, self.wl.frac_bits)
+            self._map_ready.record(main)
             self.params.seed = camera_seed(self.wl.seed, k)
-            rgb = self.camera.run()
-            L.check(lib.splat_image_accumulate(_ptr(self.out), _ptr(rgb), self.n_values, k, _stream()))
+            rgb = self.camera.run(cam.cuda_stream, self._map_ready)
+            L.check(lib.splat_image_accumulate(_ptr(self.out), _ptr(rgb), self.n_values, k, cam.cuda_stream))
+            self._shaded.record(cam)
+        main.wait_event(self._shaded)
         return self.out
