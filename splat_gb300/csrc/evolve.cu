@@ -140,7 +140,9 @@ __device__ __forceinline__ void add_stats(splat_trace_stats_t* st, int diffuse, 
 // MODE 0: plugin (retired rays written back to the caller's AoS array);
 // 1: trace (diffuse rays final-evolved into the splat queue, escaped rays
 // dropped); 2: camera (as trace, escaped rays queued unchanged for the sky).
-template <int MODE>
+// MK >= 0: the material kind, fixed at compile time so that only that
+// material's optics is inlined (smaller code, no per-evaluation switch).
+template <int MODE, int MK>
 __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
     constexpr bool TRACE = MODE != 0;
     constexpr bool SKY = MODE == 2;
@@ -172,8 +174,9 @@ __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
         if (k < n) {
             r = load_ray(A.in, k);
             id = A.in.id[k];
-            const EvolveView v{A.tris, A.n_tris, A.err, A.first_diffuse, A.material, A.seed, A.bounce,
-                               A.force_rand, quirks, A.last != 0};
+            EvolveView v{A.tris, A.n_tris, A.err, A.first_diffuse, A.material, A.seed, A.bounce,
+                         A.force_rand, quirks, A.last != 0};
+            if (MK >= 0) v.material.kind = MK;
             const int fate = evolve_one<TRACE>(r, A.hit_idx[k], id, v, o, ih);
             keep = fate == kFateKeep;
             dif = fate == kFateDiffuse;
@@ -230,25 +233,30 @@ static int evolve_grid(int64_t cap, int sm_count) {
     return (int)(b < 1 ? 1 : b);
 }
 
-cudaError_t launch_evolve_trace(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s) {
+template <int MODE>
+static cudaError_t launch_evolve_mode(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s) {
     if (cap <= 0) return cudaSuccess;
-    evolve_kernel<1><<<evolve_grid(cap, sm_count), kEvolveThreads, 0, s>>>(a);
+    const int grid = evolve_grid(cap, sm_count);
+    switch (a.material.kind) {
+        case SPLAT_MATERIAL_LINEAR_REF: evolve_kernel<MODE, SPLAT_MATERIAL_LINEAR_REF><<<grid, kEvolveThreads, 0, s>>>(a); break;
+        case SPLAT_MATERIAL_CAUCHY: evolve_kernel<MODE, SPLAT_MATERIAL_CAUCHY><<<grid, kEvolveThreads, 0, s>>>(a); break;
+        case SPLAT_MATERIAL_SELLMEIER: evolve_kernel<MODE, SPLAT_MATERIAL_SELLMEIER><<<grid, kEvolveThreads, 0, s>>>(a); break;
+        default: evolve_kernel<MODE, -1><<<grid, kEvolveThreads, 0, s>>>(a); break;
+    }
     ++g_launches;
     return cudaGetLastError();
+}
+
+cudaError_t launch_evolve_trace(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s) {
+    return launch_evolve_mode<1>(a, cap, sm_count, s);
 }
 
 cudaError_t launch_evolve_camera(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s) {
-    if (cap <= 0) return cudaSuccess;
-    evolve_kernel<2><<<evolve_grid(cap, sm_count), kEvolveThreads, 0, s>>>(a);
-    ++g_launches;
-    return cudaGetLastError();
+    return launch_evolve_mode<2>(a, cap, sm_count, s);
 }
 
 cudaError_t launch_evolve_plugin(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s) {
-    if (cap <= 0) return cudaSuccess;
-    evolve_kernel<0><<<evolve_grid(cap, sm_count), kEvolveThreads, 0, s>>>(a);
-    ++g_launches;
-    return cudaGetLastError();
+    return launch_evolve_mode<0>(a, cap, sm_count, s);
 }
 
 // evolve_ray broadcast (src/tracer.jl:181-201: `rays .= evolve_ray.(rays,
