@@ -985,6 +985,7 @@ struct splat_batch {
     std::vector<int64_t> rays;
     std::vector<int32_t> start, depth;
     std::vector<uint8_t> brute;  // item runs the per-ray brute-force hitter
+    std::vector<int32_t> mat_kind;  // item's material kind
     std::vector<void*> maps;
     std::vector<size_t> map_bytes;
     std::vector<uint8_t> zero_map;
@@ -1041,12 +1042,14 @@ splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done
     int64_t fresh_rays = 0, cap_rays = 0;
     int32_t nd = 0;
     bool any_brute = false;
+    int32_t kind = -2;  // material kind shared by every item in flight; -1 mixed
     for (int32_t s = 0; s < b->max_items; ++s) {
         if (!b->used[(size_t)s]) continue;
         const int32_t st0 = b->start[(size_t)s], last = st0 + b->depth[(size_t)s] - 1;
         if (b->tick < st0 || b->tick > last) continue;
         cap_rays += b->rays[(size_t)s];
         any_brute = any_brute || b->brute[(size_t)s];
+        kind = kind == -2 || kind == b->mat_kind[(size_t)s] ? b->mat_kind[(size_t)s] : -1;
         if (b->tick == st0) {
             fresh_rays += b->rays[(size_t)s];
             if (b->zero_map[(size_t)s])
@@ -1081,6 +1084,7 @@ splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done
         a.err = b->d_err;
         a.sm_count = sm_count_current();
         a.any_brute = any_brute;
+        a.material_kind = kind < 0 ? -1 : kind;
         a.fetch = reinterpret_cast<unsigned long long*>(&b->counts[3]);
         SPLAT_CUDA(launch_batch_tick(a, st), "batch tick");
         b->parity ^= 1;
@@ -1144,6 +1148,7 @@ splat_status_t splat_batch_create(int32_t max_items, int64_t max_pool_rays, spla
     b->start.assign((size_t)max_items, -1);
     b->depth.assign((size_t)max_items, 0);
     b->brute.assign((size_t)max_items, 0);
+    b->mat_kind.assign((size_t)max_items, -1);
     b->maps.assign((size_t)max_items, nullptr);
     b->map_bytes.assign((size_t)max_items, 0);
     b->zero_map.assign((size_t)max_items, 0);
@@ -1208,6 +1213,7 @@ splat_status_t splat_batch_admit(splat_batch_t* b, const splat_scene_t* scene, c
     b->start[(size_t)slot] = b->tick;
     b->depth[(size_t)slot] = P->depth;
     b->brute[(size_t)slot] = (!bvh || !scene->d_nodes4) ? 1 : 0;
+    b->mat_kind[(size_t)slot] = P->material.kind;
     b->maps[(size_t)slot] = d_map;
     b->map_bytes[(size_t)slot] = (size_t)P->map_w * P->map_h * (P->n_lambda > 0 ? P->n_lambda : 1) * 4;
     b->zero_map[(size_t)slot] = P->zero_map ? 1 : 0;

@@ -155,6 +155,9 @@ __global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t
 
 constexpr int kBatchThreads = 256;
 
+// MK >= 0: every item in flight has this material kind (compile-time, so
+// only its optics is inlined); -1: per item.
+template <int MK>
 __global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, RaySoA out, RaySoA queue,
                                                                      const int64_t* __restrict__ in_count,
                                                                      int64_t* out_count, int64_t* queue_count,
@@ -183,8 +186,9 @@ __global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, 
             id = in.id[k];
             const BatchItem& it = items[id >> kSlotShift];
             const uint32_t bounce = (uint32_t)(tick - it.start_tick + 1);
-            const EvolveView v{it.ftri, it.n_tris, err, it.first_diffuse, it.material, it.gen.seed, bounce,
-                               it.force_rand, it.quirks != 0, (int)bounce >= it.depth};
+            EvolveView v{it.ftri, it.n_tris, err, it.first_diffuse, it.material, it.gen.seed, bounce,
+                         it.force_rand, it.quirks != 0, (int)bounce >= it.depth};
+            if (MK >= 0) v.material.kind = MK;
             int32_t ih;
             const uint32_t grid_id = (uint32_t)(it.gen.ray_begin + (id & kLocalMask));
             const int fate = evolve_one<true>(r, hit_idx[k], grid_id, v, o, ih);
@@ -299,8 +303,17 @@ cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s) {
                                                     a.sm_count, 128, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]),
                                       128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch);
         ++g_launches;
-        batch_evolve_kernel<<<grid_cap(a.cap_rays, kBatchThreads, a.sm_count, 8), kBatchThreads, 0, s>>>(
-            a.cur, a.next, a.queue, a.cur_count, a.next_count, a.queue_count, items, a.tick, a.hit_idx, a.err);
+        const int eg = grid_cap(a.cap_rays, kBatchThreads, a.sm_count, 8);
+#define SPLAT_BATCH_EVOLVE(MK)                                                                            \
+    batch_evolve_kernel<MK><<<eg, kBatchThreads, 0, s>>>(a.cur, a.next, a.queue, a.cur_count, a.next_count, \
+                                                         a.queue_count, items, a.tick, a.hit_idx, a.err)
+        switch (a.material_kind) {
+            case SPLAT_MATERIAL_LINEAR_REF: SPLAT_BATCH_EVOLVE(SPLAT_MATERIAL_LINEAR_REF); break;
+            case SPLAT_MATERIAL_CAUCHY: SPLAT_BATCH_EVOLVE(SPLAT_MATERIAL_CAUCHY); break;
+            case SPLAT_MATERIAL_SELLMEIER: SPLAT_BATCH_EVOLVE(SPLAT_MATERIAL_SELLMEIER); break;
+            default: SPLAT_BATCH_EVOLVE(-1); break;
+        }
+#undef SPLAT_BATCH_EVOLVE
         ++g_launches;
         if (g_tune[SPLAT_TUNE_SPLAT_AGGREGATE])
             batch_splat_agg_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count,

@@ -233,6 +233,7 @@ struct BatchTickArgs {
     int32_t* err;
     int sm_count;
     bool any_brute;      // some item in flight uses the brute-force hitter (or has no BVH)
+    int material_kind;   // material kind shared by every item in flight, -1 when mixed
     unsigned long long* fetch;  // zeroed work counter of this tick's hit kernel
 };
 
