@@ -387,6 +387,7 @@ def run_ours(args):
         "clocks": clocks,
     }
 
+    out["hit_t_vs_fp64"] = hit_t_vs_fp64(step, wl)
     if not args.no_e2e:
         out["e2e"] = e2e_pipelined(step, wl, K, W, stream, world, rank)
         out["e2e"]["one_frame_at_a_time"] = e2e(step, wl, K, W, stream, world, rank)
@@ -396,6 +397,28 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def hit_t_vs_fp64(step, wl, n_sample: int = 1 << 16) -> dict:
+    """The binary32 hit distances of the workload's first bounce (the fused
+    step's hitter through splat_next_hit) against distance_to_plane
+    (src/geo.jl:433-443) re-evaluated in binary64 on the chosen triangle."""
+    from splat_gb300 import tracer
+
+    hitter = {"brute": tracer.BRUTE, "bvh2": tracer.BVH2}.get(wl.hitter, tracer.BVH)
+    d_rays = tracer.rays_from_light(wl.light, wl.upscale, wl.lambda_mode, seed=wl.seed)
+    hit, t = tracer.next_hit(step.scene, hitter, d_rays, with_t=True)
+    rays = tracer.rays_to_host(d_rays)
+    hit, t = hit.cpu().numpy(), t.cpu().numpy()
+    idx = np.nonzero(hit > 1)[0]
+    idx = idx[:: max(1, idx.size // n_sample)][:n_sample]
+    tri = wl.tris[hit[idx] - 1].astype(np.float64)
+    o, d = rays["pos"][idx].astype(np.float64), rays["dir"][idx].astype(np.float64)
+    n, a = tri[:, 0], tri[:, 1]
+    t64 = ((n * a).sum(1) - (n * o).sum(1)) / (n * d).sum(1)
+    rel = np.abs(t[idx].astype(np.float64) - t64) / np.abs(t64)
+    return {"rays": int(idx.size), "median_rel": float(np.median(rel)), "p99_rel": float(np.percentile(rel, 99)),
+            "max_rel": float(rel.max())}
 
 
 def e2e(step, wl, K, W, stream, world, rank):
