@@ -454,6 +454,30 @@ splat_status_t splat_batch_status(const splat_batch_t* batch, int32_t* in_flight
 splat_status_t splat_batch_capture(splat_batch_t* batch, void* stream, int32_t* n_ticks);
 splat_status_t splat_batch_replay(splat_batch_t* batch, const uint64_t* seeds, int32_t n_seeds, void* stream);
 
+/* ---------------------------------------------------------------- server */
+/* Continuous-batching render server over one batch engine (the served form).
+ * splat_server_submit queues a request (a resident caller-owned scene, trace
+ * parameters, a caller-owned device light map) in arrival order;
+ * splat_server_step admits what fits -- a free slot, room in the engine's
+ * ray pool, and the request's light map within map_budget_bytes of maps in
+ * flight -- and enqueues one tick on the stream, staying at most
+ * max_ticks_ahead ticks ahead of the device.  splat_server_poll returns the
+ * requests whose maps are complete (block != 0: waits for every request
+ * already given its last tick) with their completion time on the device, in
+ * ms since the server's first step.  A request's map is the one
+ * splat_trace_forward produces alone. */
+typedef struct splat_server splat_server_t;
+splat_status_t splat_server_create(int32_t max_items, int64_t max_pool_rays, int64_t map_budget_bytes,
+                                   int32_t max_ticks_ahead, splat_server_t** out);
+splat_status_t splat_server_destroy(splat_server_t* server);
+splat_status_t splat_server_submit(splat_server_t* server, const splat_scene_t* scene,
+                                   const splat_trace_params_t* params, void* d_map, int64_t* request_id);
+splat_status_t splat_server_step(splat_server_t* server, void* stream, int32_t* in_flight, int32_t* queued);
+splat_status_t splat_server_poll(splat_server_t* server, int32_t block, int64_t* request_ids, double* device_ms,
+                                 int32_t max_ids, int32_t* n_ids);
+splat_status_t splat_server_status(const splat_server_t* server, int32_t* queued, int32_t* in_flight,
+                                   int64_t* map_bytes_in_use);
+
 /* ---------------------------------------------------------------- tuning */
 /* Launch-shape knobs (process-wide): blocks per SM of the grid-stride
  * kernels (1..256), and the splat's block-level texel aggregation (0 or 1).

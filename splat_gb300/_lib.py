@@ -135,6 +135,12 @@ SIGNATURES = {
     "splat_batch_status": ([vp, C.POINTER(C.c_int32), C.POINTER(C.c_int64), C.POINTER(C.c_int32)], i32),
     "splat_batch_capture": ([vp, vp, C.POINTER(C.c_int32)], i32),
     "splat_batch_replay": ([vp, vp, i32, vp], i32),
+    "splat_server_create": ([i32, i64, i64, i32, vp], i32),
+    "splat_server_destroy": ([vp], i32),
+    "splat_server_submit": ([vp, vp, C.POINTER(TraceParams), vp, vp], i32),
+    "splat_server_step": ([vp, vp, vp, vp], i32),
+    "splat_server_poll": ([vp, i32, vp, vp, i32, vp], i32),
+    "splat_server_status": ([vp, vp, vp, vp], i32),
     "splat_set_tuning": ([i32, i32], i32),
     "splat_get_tuning": ([i32], i32),
     "splat_profile_create": ([i32, vp], i32),

@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libsplat.so")
 ROOT = os.path.dirname(HERE)
 
 CU_SOURCES = ["api.cu", "hit.cu", "evolve.cu", "batch.cu", "shade.cu", "lbvh.cu"]
-CPP_SOURCES = ["bvh_build.cpp", "mesh.cpp"]
+CPP_SOURCES = ["bvh_build.cpp", "mesh.cpp", "serve.cpp"]
 HEADERS = ["common.cuh", "optics.cuh", "kernels.h", "bvh_build.h", "hitcore.cuh", "mesh.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

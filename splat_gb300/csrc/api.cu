@@ -232,6 +232,10 @@ static splat_status_t scene_pack(splat_scene* s, cudaStream_t st) {
     return SPLAT_OK;
 }
 
+namespace splat {
+splat_status_t set_error(splat_status_t code, const std::string& msg) { return fail(code, msg); }
+}  // namespace splat
+
 extern "C" {
 
 int32_t splat_abi_version(void) { return SPLAT_ABI_VERSION; }

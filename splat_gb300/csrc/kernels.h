@@ -1,6 +1,8 @@
 // kernels.h -- host-side launchers shared by the translation units.
 #pragma once
 
+#include <string>
+
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -238,6 +240,8 @@ struct BatchTickArgs {
 };
 
 cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s);
+// sets splat_last_error() of the calling thread and returns code (api.cu)
+splat_status_t set_error(splat_status_t code, const std::string& msg);
 size_t batch_item_bytes();
 size_t batch_fresh_bytes();
 void batch_fill_item(void* dst, const BatchSceneRef& sc, const GenParams& gen, int64_t n_rays, int32_t depth,

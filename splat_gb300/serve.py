@@ -9,9 +9,13 @@ tick -- requests arriving while others are on the GPU overlap with them
 light map of a request is device memory owned by the request until it is
 delivered.
 
-Latency is measured on the device clock: an event recorded at start-up and
-one after each request's last tick give its completion time on the host
-clock, from which the arrival time is subtracted.
+The queue, admission, tick loop and completion tracking are native
+(splat_server_*, csrc/serve.cpp); this module keeps the scene pool and maps
+arrivals on the host clock to submissions.
+
+Latency is measured on the device clock: the native server's start event and
+the event after each request's last tick give its completion time on the
+host clock, from which the arrival time is subtracted.
 """
 from __future__ import annotations
 
@@ -91,31 +95,45 @@ class ScenePool:
 
 
 class Server:
-    """Continuous-batching renderer over one batch engine."""
+    """Continuous-batching renderer: the native server (splat_server_*: arrival
+    order, admission by engine slot, ray-pool room and light-map budget, one
+    tick per step, bounded run-ahead, completion on the device) with scenes
+    kept resident by a ScenePool.  A request is handed to the native server
+    once it has arrived on the host clock, with its scene acquired; the scene
+    is released when the request completes."""
 
     def __init__(self, scenes: ScenePool, budget_bytes: int, max_items: int = 128, max_pool_rays: int = 1 << 26,
                  max_ticks_ahead: int = 4):
+        import ctypes as C
+
         import torch
 
-        self.torch = torch
+        from . import _lib as L
+
+        self.torch, self.C, self.L = torch, C, L
+        self.lib = L.load()
         self.scenes = scenes
         self.budget = int(budget_bytes)
-        self.engine = B.Batch(max_items, max_pool_rays)
         self.engine_bytes = B.Batch.device_bytes(max_items, max_pool_rays)
-        self.max_pool_rays = int(max_pool_rays)
+        self.max_items = int(max_items)
+        h = C.c_void_p()
+        L.check(self.lib.splat_server_create(int(max_items), int(max_pool_rays),
+                                             max(0, self.budget - self.engine_bytes), int(max_ticks_ahead),
+                                             C.byref(h)))
+        self.handle = h
         self.stream = torch.cuda.current_stream()
         self.map_bytes_in_use = 0
-        self.inflight: Dict[int, Request] = {}
+        self.inflight: Dict[int, Request] = {}   # native request id -> request
         self.pending: List[Request] = []
         self.done: List[Request] = []
-        self.max_ticks_ahead = max_ticks_ahead
-        self._tick_events = collections.deque()
-        self.ev0 = torch.cuda.Event(enable_timing=True)
+        self._ids = (C.c_int64 * 256)()
+        self._ms = (C.c_double * 256)()
+        # the server's device clock starts at its first step; the host clock
+        # is read right after it, with the stream idle
         torch.cuda.synchronize()
-        self.ev0.record(self.stream)
+        self._native_step()
         torch.cuda.synchronize()
         self.host0 = time.perf_counter()
-        self._completion = []  # (event, request)
 
     def now(self) -> float:
         return time.perf_counter() - self.host0
@@ -123,76 +141,80 @@ class Server:
     def submit(self, req: Request) -> None:
         heapq.heappush(self.pending, req)
 
-    def _try_admit(self, req: Request) -> bool:
-        mb = map_bytes(req.wl)
-        other = self.engine_bytes + self.map_bytes_in_use + mb
-        sc = self.scenes.acquire(req.scene_id, other)
-        if sc is None:
-            return False
-        tex = tracer.new_light_map(req.wl.map_w, req.wl.map_h, req.wl.n_planes, req.wl.accum)
-        try:
-            slot = self.engine.admit(sc, req.wl, tex)
-        except B.PoolFull:
-            self.scenes.release(req.scene_id)
-            del tex
-            return False
-        req.tex = tex
-        self.map_bytes_in_use += mb
-        self.inflight[slot] = req
-        return True
+    def _native_step(self):
+        C = self.C
+        fl, q = C.c_int32(), C.c_int32()
+        self.L.check(self.lib.splat_server_step(self.handle, self.stream.cuda_stream, C.byref(fl), C.byref(q)))
+        return fl.value, q.value
 
-    def step(self) -> int:
-        """Admits what has arrived and fits, enqueues one tick; returns the
-        number of requests completed on the device so far."""
-        self._collect()
+    def _arrive(self) -> None:
+        """Hands every request that has arrived to the native server."""
+        from . import tracer
+
+        C = self.C
         t = self.now()
         while self.pending and self.pending[0].arrival <= t:
-            if not self._try_admit(self.pending[0]):
-                if not self.inflight:
-                    if not self._completion:
-                        raise RuntimeError(f"request {self.pending[0].rid} can never fit the budget or the pool")
-                    self._collect(block=True)  # room held only by delivered-but-uncollected maps
-                    continue
-                break
+            req = self.pending[0]
+            mb = map_bytes(req.wl)
+            sc = self.scenes.acquire(req.scene_id, self.engine_bytes + self.map_bytes_in_use + mb)
+            if sc is None:
+                return  # its scene fits only after requests in flight release theirs
             heapq.heappop(self.pending)
-        if self.engine.status()["in_flight"] == 0:
-            return len(self.done)
-        # keep the host at most a few ticks ahead of the device
-        while len(self._tick_events) >= self.max_ticks_ahead:
-            self._tick_events.popleft().synchronize()
-        finished = self.engine.tick(self.stream.cuda_stream)
-        ev = self.torch.cuda.Event(enable_timing=True)
-        ev.record(self.stream)
-        self._tick_events.append(ev)
-        for slot in finished:
-            req = self.inflight.pop(slot)
-            self._completion.append((ev, req, slot))
+            req.tex = tracer.new_light_map(req.wl.map_w, req.wl.map_h, req.wl.n_planes, req.wl.accum)
+            P = tracer.trace_params(req.wl)
+            rid = C.c_int64()
+            self.L.check(self.lib.splat_server_submit(self.handle, sc.handle, C.byref(P), req.tex.data_ptr(),
+                                                      C.byref(rid)))
+            self.inflight[int(rid.value)] = req
+            self.map_bytes_in_use += mb
+
+    def step(self) -> int:
+        """Hands over what has arrived, enqueues one tick; returns the number
+        of requests completed so far."""
+        self._arrive()
+        self._native_step()
         self._collect()
         return len(self.done)
 
     def _collect(self, block: bool = False) -> None:
-        keep = []
-        for ev, req, slot in self._completion:
-            if block or ev.query():
-                ev.synchronize()
-                req.done_at = self.ev0.elapsed_time(ev) / 1e3
-                self.engine.release(slot)
+        C = self.C
+        while True:
+            n = C.c_int32()
+            self.L.check(self.lib.splat_server_poll(self.handle, int(block), self._ids, self._ms, len(self._ids),
+                                                    C.byref(n)))
+            for i in range(n.value):
+                req = self.inflight.pop(int(self._ids[i]))
+                req.done_at = self._ms[i] / 1e3
                 self.scenes.release(req.scene_id)
                 self.map_bytes_in_use -= map_bytes(req.wl)
                 self.done.append(req)
-            else:
-                keep.append((ev, req, slot))
-        self._completion = keep
+            if n.value < len(self._ids):
+                return
 
     def drain(self) -> None:
         while self.pending or self.inflight:
             if not self.inflight and self.pending and self.pending[0].arrival > self.now():
                 time.sleep(max(0.0, min(0.001, self.pending[0].arrival - self.now())))
+            if self.pending and not self.inflight and self.pending[0].arrival <= self.now():
+                self._arrive()
+                if not self.inflight:
+                    raise RuntimeError(f"request {self.pending[0].rid} can never fit the budget")
             self.step()
         self._collect(block=True)
 
     def latencies(self) -> np.ndarray:
         return np.array([r.done_at - r.arrival for r in self.done])
+
+    def close(self) -> None:
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.splat_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def poisson_arrivals(rate: float, duration: float, seed: int) -> np.ndarray:

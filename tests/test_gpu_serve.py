@@ -42,3 +42,58 @@ def test_served_results_equal_alone():
     for r in srv.done:
         alone = tracer.trace_forward(r.wl, scene=pool.resident[r.scene_id]).tex
         assert torch.equal(r.tex, alone), f"request {r.rid} differs from its alone result"
+
+
+def test_native_server_budget_and_order():
+    """splat_server_* directly: with a map budget that holds one request's map
+    at a time, requests still complete, one after another, in arrival order,
+    each equal to its alone result; a map larger than the budget is refused
+    at submission."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import ctypes as C
+
+    from splat_gb300 import _lib as L
+    from splat_gb300 import tracer
+
+    lib = L.load()
+    tris, fd = S.assemble(S.sphere_tris(3, noise_amp=0.05), S.floor_tris(-1.5, 4.0))
+    scene = tracer.Scene(tris, fd, bvh=True)
+    wls = [S.Workload(name=f"q{i}", tris=tris, first_diffuse=fd, light=S.hemisphere_light(i, 96, 1.1), depth=3,
+                      spectrum=S.stratified_spectrum(4), lambda_mode=(T.LAMBDA_STRATIFIED, 4, 400.0, 700.0),
+                      material=S.CAUCHY_GLASS, map_w=64, map_h=64, accum="i32", hitter="bvh", seed=90 + i)
+           for i in range(5)]
+    one_map = 64 * 64 * 4 * 4
+    h = C.c_void_p()
+    L.check(lib.splat_server_create(8, 1 << 20, one_map, 2, C.byref(h)))
+    try:
+        stream = torch.cuda.current_stream().cuda_stream
+        texs, ids = [], []
+        for wl in wls:
+            tex = tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum)
+            P = tracer.trace_params(wl)
+            rid = C.c_int64()
+            L.check(lib.splat_server_submit(h, scene.handle, C.byref(P), tex.data_ptr(), C.byref(rid)))
+            texs.append(tex)
+            ids.append(rid.value)
+        big = wls[0].with_(map_w=128)
+        P = tracer.trace_params(big)
+        rid = C.c_int64()
+        assert lib.splat_server_submit(h, scene.handle, C.byref(P), texs[0].data_ptr(), C.byref(rid)) == L.ERR_WORKSPACE
+        order = []
+        buf, ms = (C.c_int64 * 16)(), (C.c_double * 16)()
+        for _ in range(1000):
+            fl, q, n = C.c_int32(), C.c_int32(), C.c_int32()
+            L.check(lib.splat_server_step(h, stream, C.byref(fl), C.byref(q)))
+            assert fl.value <= 1  # one map in flight at a time
+            # nothing ticking: wait for the completions that hold the budget
+            L.check(lib.splat_server_poll(h, int(fl.value == 0), buf, ms, 16, C.byref(n)))
+            order += [buf[i] for i in range(n.value)]
+            if len(order) == len(wls):
+                break
+        assert order == ids
+        for wl, tex in zip(wls, texs):
+            assert torch.equal(tex, tracer.trace_forward(wl, scene=scene).tex)
+    finally:
+        lib.splat_server_destroy(h)
