@@ -723,12 +723,31 @@ struct SideStream {
 };
 }  // namespace
 
+// At most kSideStreams per host thread: a caller that cycles through many
+// short-lived streams gets the least recently used side stream destroyed
+// (CUDA releases a stream and its events once their pending work is done).
+constexpr size_t kSideStreams = 32;
+
 static cudaError_t side_stream_for(cudaStream_t caller, SideStream** out) {
-    thread_local std::map<std::pair<int, cudaStream_t>, SideStream> streams;
+    thread_local std::map<std::pair<int, cudaStream_t>, std::pair<uint64_t, SideStream>> streams;
+    thread_local uint64_t clock = 0;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    SideStream& x = streams[{dev, caller}];
+    const std::pair<int, cudaStream_t> key{dev, caller};
+    if (streams.find(key) == streams.end() && streams.size() >= kSideStreams) {
+        auto lru = streams.begin();
+        for (auto it = streams.begin(); it != streams.end(); ++it)
+            if (it->second.first < lru->second.first) lru = it;
+        SideStream& old = lru->second.second;
+        for (cudaEvent_t ev : old.ev)
+            if (ev) cudaEventDestroy(ev);
+        if (old.s) cudaStreamDestroy(old.s);
+        streams.erase(lru);
+    }
+    auto& entry = streams[key];
+    entry.first = ++clock;
+    SideStream& x = entry.second;
     if (!x.s) {
         if ((e = cudaStreamCreateWithFlags(&x.s, cudaStreamNonBlocking)) != cudaSuccess) return e;
         for (cudaEvent_t& ev : x.ev)

@@ -197,3 +197,21 @@ def test_splat_overlap_matches_single_splat(torch_cuda, accum, overlap):
     ref_tex, ref_st, _ = O.trace_forward(wl, lo, lo + 1000)
     assert st["rays_per_bounce"] == [int(x) for x in ref_st[: wl.depth]]
     _cmp(wl, got, ref_tex)
+
+
+def test_many_caller_streams(torch_cuda):
+    """The fused step on more caller streams than the library keeps side
+    streams for (the least recently used are recycled): every map equals the
+    one on the default stream."""
+    from splat_gb300 import tracer
+
+    wl = S.realtime(light=S.scaled_light(S.realtime().light, 256))
+    scene = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
+    ref = tracer.trace_forward(wl, scene=scene).tex.clone()
+    streams = [torch_cuda.cuda.Stream() for _ in range(40)]
+    outs = []
+    for s in streams:
+        with torch_cuda.cuda.stream(s):
+            outs.append(tracer.trace_forward(wl, scene=scene).tex)
+    torch_cuda.cuda.synchronize()
+    assert ref.sum() > 0 and all(torch_cuda.equal(o, ref) for o in outs)
