@@ -489,3 +489,110 @@ def translate(tris: np.ndarray, offset) -> np.ndarray:
     out = tris.copy()
     out[:, 1:4] = (out[:, 1:4] + np.asarray(offset, np.float32)).astype(np.float32)
     return out
+
+
+def scale(tris: np.ndarray, s: float) -> np.ndarray:
+    """scale(t::FTri, s) (src/geo.jl:137-138): vertices scaled; the plane
+    normal, vertex normals and uvs kept."""
+    out = tris.copy()
+    out[:, 1:4] = (out[:, 1:4] * np.float32(s)).astype(np.float32)
+    return out
+
+
+def rotate(tris: np.ndarray, R) -> np.ndarray:
+    """rotate(t::FTri, R) (src/geo.jl:139-150): plane normal, vertices and
+    vertex normals multiplied by the 3 x 3 matrix R; uvs kept."""
+    out = tris.copy()
+    R = np.asarray(R, np.float32)
+    out[:, 0:7] = np.einsum("ij,tkj->tki", R, out[:, 0:7]).astype(np.float32)
+    return out
+
+
+def _ftri(n, a, b, c, na, nb, nc, ta, tb, tc) -> np.ndarray:
+    return np.stack([n, a, b, c, na, nb, nc, ta, tb, tc], 1).astype(np.float32)
+
+
+def _cross32(u: np.ndarray, v: np.ndarray) -> np.ndarray:
+    u, v = u.astype(np.float32), v.astype(np.float32)
+    return np.stack([u[:, 1] * v[:, 2] - u[:, 2] * v[:, 1], u[:, 2] * v[:, 0] - u[:, 0] * v[:, 2],
+                     u[:, 0] * v[:, 1] - u[:, 1] * v[:, 0]], 1).astype(np.float32)
+
+
+def square() -> np.ndarray:
+    """square() (src/procedural_assets.jl:76-84): the unit square at z = 0 as
+    two triangles facing +z, uv = position."""
+    a, b, c, d = (np.array(v, np.float32)[None] for v in ((0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0)))
+    n = np.array([[0, 0, 1]], np.float32)
+    return np.concatenate([_ftri(n, a, b, c, n, n, n, a, b, c), _ftri(n, b, c, d, n, n, n, b, c, d)], 0)
+
+
+def stage() -> np.ndarray:
+    """stage() (src/procedural_assets.jl:1-18): a floor triangle at z = -2
+    and two walls meeting at (0, -2, 2), flat-shaded."""
+    p = lambda *v: np.array([v], np.float32)  # noqa: E731
+    a, b, c, d = p(3, 1, -2), p(-3, 1, -2), p(0, -2, -2), p(0, -2, 2)
+    ta, tb, tc, td = p(0, 0, 0), p(1, 0, 0), p(0.5, 0.5, 0), p(0.5, 1, 0)
+
+    def unit(v):
+        return (v / np.sqrt((v.astype(np.float32) ** 2).sum(1, keepdims=True))).astype(np.float32)
+
+    n1 = unit(_cross32(a - b, a - c))
+    n2 = unit(_cross32(d - b, d - c))
+    n3 = unit(_cross32(d - a, d - c))
+    return np.concatenate([_ftri(n1, a, b, c, n1, n1, n1, ta, tb, tc), _ftri(n2, b, c, d, n2, n2, n2, tb, tc, td),
+                           _ftri(n3, a, d, c, n3, n3, n3, ta, td, tc)], 0)
+
+
+def ripples(t: float = 0.0, step: float = 0.005) -> np.ndarray:
+    """ripples(t) (src/procedural_assets.jl:20-73): a water surface over the
+    unit square, height f(x, y) = (s(50, x) + s(60, x) + s(70, y) + s(80, y))
+    * 1.25e-4 with s(k, u) = sin(k u - k tanh(k) t), two triangles per grid
+    cell, vertex normals (df/dx, df/dy, -1), uv = (x, y, 0).  The values are
+    evaluated in binary64 and stored as binary32; the order of the triangles
+    is the reference's (per grid row y, the first triangles of every x, then
+    the second ones)."""
+    n = int(round(1.0 / step))
+    x = np.arange(n, dtype=np.float64) * step
+    om = lambda k: k * np.tanh(k)  # noqa: E731
+
+    def f(x, y):
+        s = lambda k, u: np.sin(k * u - om(k) * t)  # noqa: E731
+        return (s(50, x) + s(60, x) + s(70, y) + s(80, y)) * 0.000125
+
+    def nrm(x, y):
+        c = lambda k, u: np.cos(k * u - om(k) * t) * k  # noqa: E731
+        return np.stack([(c(50, x) + c(60, x)) * 0.000125, (c(70, y) + c(80, y)) * 0.000125,
+                         -np.ones_like(x)], -1).astype(np.float32)
+
+    def vert(x, y):
+        return np.stack([x, y, f(x, y)], -1).astype(np.float32)
+
+    X, Y = np.meshgrid(x, x, indexing="xy")  # rows: y, columns: x
+    X, Y = X.reshape(-1), Y.reshape(-1)
+    dx = dy = step
+
+    def tri(pa, pb, pc):
+        a, b, c = vert(*pa), vert(*pb), vert(*pc)
+        ta, tb, tc = (np.stack([v[:, 0], v[:, 1], np.zeros_like(v[:, 0])], 1) for v in (a, b, c))
+        return _ftri(_cross32(a - b, a - c), a, b, c, nrm(*pa), nrm(*pb), nrm(*pc), ta, tb, tc)
+
+    t1 = tri((X, Y), (X + dx, Y), (X, Y + dy)).reshape(n, n, 10, 3)
+    t2 = tri((X + dx, Y + dy), (X + dx, Y), (X, Y + dy)).reshape(n, n, 10, 3)
+    return np.ascontiguousarray(np.concatenate([t1, t2], 1).reshape(-1, 10, 3))
+
+
+def ripples_scene(t: float = 0.0, **kw) -> Workload:
+    """The reference's ripples scene (src/scenes/ripples.jl:21-32): the water
+    surface (glass) centred on the origin over the unit square three units
+    below it (diffuse), lit from above; 80,000 water triangles.  Caustics of
+    a moving surface: ripples_scene(t) at successive t are the frames of an
+    animation."""
+    rips = translate(ripples(t), (-0.5, -0.5, 0.0))
+    sq = translate(square(), (-0.5, -1.0, -3.0))
+    tris, fd = assemble_meshes([rips], [sq])
+    light = T.rect_light((0.0, 0.0, 2.0), (0.0, 0.0, -1.0), (0.6, 0.0, 0.0), (0.0, 0.6, 0.0), 1024, 1024)
+    w = Workload(name="ripples-80000tris-2^20rays-depth2-bvh-512x512-i32", tris=tris, first_diffuse=fd, light=light,
+                 upscale=1, lambda_mode=(T.LAMBDA_STRATIFIED, 8, 400.0, 700.0), spectrum=stratified_spectrum(8),
+                 depth=2, material=(T.MATERIAL_CAUCHY, 1.33, 0.003), map_w=512, map_h=512, accum="i32",
+                 hitter="bvh", seed=31)
+    return w.with_(**kw) if kw else w

@@ -123,3 +123,22 @@ def test_trace_on_rebuilt_scene_equals_host_bvh(torch_cuda):
     assert np.array_equal(a.tex.cpu().numpy(), b.tex.cpu().numpy())
     c = tracer.trace_forward(wl.with_(hitter="bvh2"), scene=gpu)
     assert np.array_equal(a.tex.cpu().numpy(), c.tex.cpu().numpy())
+
+
+def test_moving_water_surface(torch_cuda):
+    """The reference's ripples scene (src/procedural_assets.jl:20-73) animated:
+    each frame's surface uploaded and the BVH rebuilt on the GPU; a sampled ray
+    range of every frame equals the oracle on that frame's geometry."""
+    from splat_gb300 import tracer
+
+    wl0 = S.ripples_scene(0.0)
+    scene = tracer.Scene(wl0.tris, wl0.first_diffuse, bvh=True)
+    n = wl0.n_rays
+    lo = n // 4 + 300  # a range of the light grid above the part of the water over the square
+    for t in (0.05, 0.1, 0.15):
+        wl = S.ripples_scene(t)
+        scene.rebuild(torch_cuda.from_numpy(np.ascontiguousarray(wl.tris).reshape(-1)).cuda())
+        r = tracer.trace_forward(wl, scene=scene, ray_begin=lo, ray_end=lo + 1400)
+        ref, ref_st, _ = O.trace_forward(wl, lo, lo + 1400)
+        assert r.stats["rays_per_bounce"] == [int(x) for x in ref_st[: wl.depth]] and ref_st[1] > 0
+        assert np.array_equal(r.tex.cpu().numpy().ravel(), ref.ravel(order="F")) and ref.sum() > 0

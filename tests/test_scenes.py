@@ -53,3 +53,35 @@ def test_spectrum():
     assert s.dtype == np.float32 and len(s) == 16
     assert abs(s[0] - (400 + 300 / 32)) < 1e-4 and abs(s[-1] - (700 - 300 / 32)) < 1e-4
     assert T.upres(2).tolist() == [-0.25, 0.25]
+
+
+def test_reference_procedural_assets():
+    """square / stage / ripples (src/procedural_assets.jl) and the FTri
+    transforms (src/geo.jl:132-150)."""
+    sq = S.square()
+    assert sq.shape == (2, 10, 3) and (sq[:, 0] == [0, 0, 1]).all()
+    np.testing.assert_array_equal(sq[1, 1:4], [[1, 0, 0], [0, 1, 0], [1, 1, 0]])
+    st = S.stage()
+    assert st.shape == (3, 10, 3)
+    np.testing.assert_allclose(np.linalg.norm(st[:, 0], axis=1), 1.0, rtol=1e-6)
+    r = S.ripples(0.3)
+    assert r.shape == (80000, 10, 3) and np.isfinite(r).all()
+    # per grid row y: 200 first triangles (x ascending), then 200 second ones
+    np.testing.assert_allclose(r[1, 1, :2], [0.005, 0.0], atol=1e-9)
+    np.testing.assert_allclose(r[200, 1, :2], [0.005, 0.005], atol=1e-9)
+    np.testing.assert_allclose(r[400, 1, :2], [0.0, 0.005], atol=1e-9)
+    # plane normals: +z for the first triangles, -z for the second (their
+    # winding, as in the reference); vertex normals (df/dx, df/dy, -1)
+    first = (np.arange(80000) // 200) % 2 == 0
+    assert (r[first, 0, 2] > 0).all() and (r[~first, 0, 2] < 0).all() and (r[:, 4:7, 2] == -1).all()
+    assert np.abs(r[:, 1:4, 2]).max() <= 4 * 0.000125 + 1e-9
+    assert not np.array_equal(S.ripples(0.0)[:, 1:4, 2], r[:, 1:4, 2])  # the surface moves with t
+    w = S.ripples_scene(0.1)
+    assert w.n_tris == 80003 and w.first_diffuse == 80002 and w.n_rays == 1 << 20
+    s2 = S.scale(sq, 2.0)
+    np.testing.assert_array_equal(s2[:, 1:4], sq[:, 1:4] * 2)
+    np.testing.assert_array_equal(s2[:, 0], sq[:, 0])
+    Rz = np.array([[0, -1, 0], [1, 0, 0], [0, 0, 1]], np.float32)
+    rot = S.rotate(st, Rz)
+    np.testing.assert_allclose(rot[:, 1:4], st[:, 1:4] @ Rz.T, atol=1e-6)
+    np.testing.assert_array_equal(rot[:, 7:10], st[:, 7:10])
