@@ -1016,6 +1016,14 @@ struct splat_batch {
     int parity = 0;
     bool dirty = true;
     cudaGraphExec_t exec = nullptr;
+    // captured graphs: the splat of tick t on a side stream beside tick t + 1
+    // (queues alternate by tick parity; q2 is allocated at the first such capture)
+    RaySoA q2{};
+    void* q2_mem = nullptr;
+    cudaStream_t side = nullptr;
+    cudaEvent_t traced_ev[2] = {nullptr, nullptr}, splat_ev[2] = {nullptr, nullptr};
+    bool splat_pending[2] = {false, false};
+    bool overlap = false;    // set while capturing with the overlap
     int32_t cap_t1 = 0;      // host tick after the captured ticks
     int cap_parity1 = 0;     // buffer parity after them
 };
@@ -1031,6 +1039,12 @@ void batch_free(splat_batch* b) {
     if (!b) return;
     if (b->exec) cudaGraphExecDestroy(b->exec);
     cudaFree(b->d_mem);
+    if (b->q2_mem) cudaFree(b->q2_mem);
+    for (int i = 0; i < 2; ++i) {
+        if (b->traced_ev[i]) cudaEventDestroy(b->traced_ev[i]);
+        if (b->splat_ev[i]) cudaEventDestroy(b->splat_ev[i]);
+    }
+    if (b->side) cudaStreamDestroy(b->side);
     for (int i = 0; i < 2; ++i) {
         if (b->h_stage[i]) cudaFreeHost(b->h_stage[i]);
         if (b->stage_ev[i]) cudaEventDestroy(b->stage_ev[i]);
@@ -1060,6 +1074,26 @@ splat_status_t batch_upload(splat_batch* b, cudaStream_t st) {
 }
 
 // Enqueues one tick (no table upload).
+// The second queue, side stream and fork / join events of a capture with
+// the splat overlap, made on first use.
+cudaError_t batch_overlap_ready(splat_batch* b) {
+    cudaError_t e = cudaSuccess;
+    if (!b->q2_mem) {
+        e = cudaMalloc(&b->q2_mem, soa_bytes(b->cap) + kAlign);
+        if (e != cudaSuccess) return e;
+        char* p = reinterpret_cast<char*>(align_up(reinterpret_cast<size_t>(b->q2_mem)));
+        b->q2 = carve_soa(p, b->cap);
+    }
+    if (!b->side && (e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking)) != cudaSuccess) return e;
+    for (int i = 0; i < 2; ++i) {
+        if (!b->traced_ev[i] && (e = cudaEventCreateWithFlags(&b->traced_ev[i], cudaEventDisableTiming)) != cudaSuccess)
+            return e;
+        if (!b->splat_ev[i] && (e = cudaEventCreateWithFlags(&b->splat_ev[i], cudaEventDisableTiming)) != cudaSuccess)
+            return e;
+    }
+    return cudaSuccess;
+}
+
 splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done_slots, int32_t max_done,
                                   int32_t* n_done) {
     int64_t fresh_rays = 0, cap_rays = 0;
@@ -1086,8 +1120,18 @@ splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done
     if (n_done) *n_done = nd;
     int64_t* cur_count = &b->counts[b->parity];
     int64_t* next_count = &b->counts[b->parity ^ 1];
+    // with the overlap, tick t splats queue (t & 1) on the side stream; the
+    // main stream reuses that queue two ticks later, after that splat
+    const int qp = b->overlap ? (b->tick & 1) : 0;
+    RaySoA queue = qp ? b->q2 : b->q;
+    int64_t* queue_count = qp ? &b->counts[5] : &b->counts[2];
+    if (b->overlap && b->splat_pending[qp]) {
+        SPLAT_CUDA(cudaStreamWaitEvent(st, b->splat_ev[qp], 0), "batch: wait for the queue's splat");
+        b->splat_pending[qp] = false;
+    }
     SPLAT_CUDA(cudaMemsetAsync(next_count, 0, sizeof(int64_t), st), "batch: reset count");
-    SPLAT_CUDA(cudaMemsetAsync(&b->counts[2], 0, 2 * sizeof(int64_t), st), "batch: reset queue + work counter");
+    SPLAT_CUDA(cudaMemsetAsync(queue_count, 0, sizeof(int64_t), st), "batch: reset queue");
+    SPLAT_CUDA(cudaMemsetAsync(&b->counts[3], 0, sizeof(int64_t), st), "batch: reset work counter");
     if (cap_rays > 0) {
         ProfScope ps(SPLAT_KERNEL_BATCH, st);
         BatchTickArgs a;
@@ -1097,10 +1141,10 @@ splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done
         a.fresh = b->d_fresh;
         a.cur = b->parity ? b->b : b->a;
         a.next = b->parity ? b->a : b->b;
-        a.queue = b->q;
+        a.queue = queue;
         a.cur_count = cur_count;
         a.next_count = next_count;
-        a.queue_count = &b->counts[2];
+        a.queue_count = queue_count;
         a.fresh_rays = fresh_rays;
         a.cap_rays = cap_rays;
         a.hit_idx = b->hit;
@@ -1109,7 +1153,16 @@ splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done
         a.any_brute = any_brute;
         a.material_kind = kind < 0 ? -1 : kind;
         a.fetch = reinterpret_cast<unsigned long long*>(&b->counts[3]);
-        SPLAT_CUDA(launch_batch_tick(a, st), "batch tick");
+        if (b->overlap) {
+            SPLAT_CUDA(launch_batch_trace(a, st), "batch tick");
+            SPLAT_CUDA(cudaEventRecord(b->traced_ev[qp], st), "batch: fork");
+            SPLAT_CUDA(cudaStreamWaitEvent(b->side, b->traced_ev[qp], 0), "batch: fork");
+            SPLAT_CUDA(launch_batch_splat(a, b->side), "batch splat");
+            SPLAT_CUDA(cudaEventRecord(b->splat_ev[qp], b->side), "batch: join");
+            b->splat_pending[qp] = true;
+        } else {
+            SPLAT_CUDA(launch_batch_tick(a, st), "batch tick");
+        }
         b->parity ^= 1;
     }
     b->tick += 1;
@@ -1300,10 +1353,18 @@ splat_status_t splat_batch_capture(splat_batch_t* b, void* stream, int32_t* n_ti
     const int32_t t0 = b->tick;
     const int p0 = b->parity;
     cudaGraph_t graph = nullptr;
+    b->overlap = g_tune[SPLAT_TUNE_SPLAT_OVERLAP] > 0 && batch_overlap_ready(b) == cudaSuccess;
+    b->splat_pending[0] = b->splat_pending[1] = false;
     SPLAT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "batch_capture: begin");
     cudaError_t e = cudaMemsetAsync(&b->counts[p0], 0, sizeof(int64_t), st);
     rc = SPLAT_OK;
     while (e == cudaSuccess && rc == SPLAT_OK && b->tick <= last) rc = batch_enqueue_tick(b, st, nullptr, 0, nullptr);
+    for (int p = 0; p < 2 && e == cudaSuccess; ++p)
+        if (b->overlap && b->splat_pending[p]) {
+            e = cudaStreamWaitEvent(st, b->splat_ev[p], 0);  // join the side stream before the capture ends
+            b->splat_pending[p] = false;
+        }
+    b->overlap = false;
     cudaError_t e2 = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess) return cuda_fail(e, "batch_capture: memset");
     if (rc != SPLAT_OK) return rc;

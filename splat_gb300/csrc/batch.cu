@@ -285,6 +285,12 @@ static int grid_cap(int64_t n, int threads, int sm_count, int per_sm) {
 }
 
 cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s) {
+    cudaError_t e = launch_batch_trace(a, s);
+    if (e != cudaSuccess) return e;
+    return launch_batch_splat(a, s);
+}
+
+cudaError_t launch_batch_trace(const BatchTickArgs& a, cudaStream_t s) {
     const BatchItem* items = reinterpret_cast<const BatchItem*>(a.items);
     FreshList* fresh = reinterpret_cast<FreshList*>(a.fresh);
     batch_reserve_kernel<<<1, kMaxBatchItems, 0, s>>>(items, a.n_slots, a.tick, a.cur_count, fresh);
@@ -315,13 +321,18 @@ cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s) {
         }
 #undef SPLAT_BATCH_EVOLVE
         ++g_launches;
-        if (g_tune[SPLAT_TUNE_SPLAT_AGGREGATE])
-            batch_splat_agg_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count,
-                                                                                           items);
-        else
-            batch_splat_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count, items);
-        ++g_launches;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_splat(const BatchTickArgs& a, cudaStream_t s) {
+    if (a.cap_rays <= 0) return cudaSuccess;
+    const BatchItem* items = reinterpret_cast<const BatchItem*>(a.items);
+    if (g_tune[SPLAT_TUNE_SPLAT_AGGREGATE])
+        batch_splat_agg_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count, items);
+    else
+        batch_splat_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count, items);
+    ++g_launches;
     return cudaGetLastError();
 }
 

@@ -240,6 +240,9 @@ struct BatchTickArgs {
 };
 
 cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s);
+// the two halves of a tick: reserve, generate, hit, evolve; and the splat of the tick's queue
+cudaError_t launch_batch_trace(const BatchTickArgs& a, cudaStream_t s);
+cudaError_t launch_batch_splat(const BatchTickArgs& a, cudaStream_t s);
 // sets splat_last_error() of the calling thread and returns code (api.cu)
 splat_status_t set_error(splat_status_t code, const std::string& msg);
 size_t batch_item_bytes();
