@@ -391,6 +391,10 @@ def run_ours(args):
     if not args.no_e2e:
         out["e2e"] = e2e_pipelined(step, wl, K, W, stream, world, rank)
         out["e2e"]["one_frame_at_a_time"] = e2e(step, wl, K, W, stream, world, rank)
+        # deeper pipelines than the reference's double buffering, for reference
+        Kd = min(K, 300)
+        out["e2e"]["frames_in_flight"] = {
+            str(m): e2e_pipelined(step, wl, Kd, W, stream, world, rank, n_sets=m)["value"] for m in (3, 4)}
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     if rank == 0:
@@ -461,7 +465,7 @@ def e2e(step, wl, K, W, stream, world, rank):
             "ms_per_step": ms / K, "api": "splat_trace_forward_host"}
 
 
-def e2e_pipelined(step, wl, K, W, stream, world, rank):
+def e2e_pipelined(step, wl, K, W, stream, world, rank, n_sets: int = 2):
     """rays/s end to end with two frames in flight, the way the reference's
     real-time loop double-buffers its trace! calls (src/scenes/sphere.jl:
     175-219).  Frames alternate between two buffer sets, each with its own
@@ -477,25 +481,26 @@ def e2e_pipelined(step, wl, K, W, stream, world, rank):
     from splat_gb300 import tracer
 
     lib = L.load()
-    scenes = [step.scene, tracer.Scene(wl.tris, wl.first_diffuse, bvh=(wl.hitter != "brute"))]
-    streams = [stream, torch.cuda.Stream()]
-    wss = [step.ws, torch.empty_like(step.ws)]
+    m = n_sets
+    scenes = [step.scene] + [tracer.Scene(wl.tris, wl.first_diffuse, bvh=(wl.hitter != "brute")) for _ in range(m - 1)]
+    streams = [stream] + [torch.cuda.Stream() for _ in range(m - 1)]
+    wss = [step.ws] + [torch.empty_like(step.ws) for _ in range(m - 1)]
     tris_pinned = torch.from_numpy(np.ascontiguousarray(wl.tris).reshape(-1)).pin_memory()
-    d_tris = [torch.empty_like(tris_pinned, device="cuda") for _ in range(2)]
-    maps = [step.tex, torch.empty_like(step.tex)]
-    stats = [torch.zeros(16, dtype=torch.int64, device="cuda") for _ in range(2)]
-    host_maps = [torch.empty(m.shape, dtype=m.dtype).pin_memory() for m in maps]
-    host_stats = [torch.zeros(16, dtype=torch.int64).pin_memory() for _ in range(2)]
+    d_tris = [torch.empty_like(tris_pinned, device="cuda") for _ in range(m)]
+    maps = [step.tex] + [torch.empty_like(step.tex) for _ in range(m - 1)]
+    stats = [torch.zeros(16, dtype=torch.int64, device="cuda") for _ in range(m)]
+    host_maps = [torch.empty(mp.shape, dtype=mp.dtype).pin_memory() for mp in maps]
+    host_stats = [torch.zeros(16, dtype=torch.int64).pin_memory() for _ in range(m)]
     copy = torch.cuda.Stream()
-    traced = [torch.cuda.Event() for _ in range(2)]
-    copied = [torch.cuda.Event() for _ in range(2)]
+    traced = [torch.cuda.Event() for _ in range(m)]
+    copied = [torch.cuda.Event() for _ in range(m)]
     P = step.params
     segs = [0]
 
     def one(i, b, first_timed):
-        if i >= 2:
-            copied[b].synchronize()  # step i - 2's map and counters are on the host: its buffers are free
-            if i - 2 >= first_timed:
+        if i >= m:
+            copied[b].synchronize()  # step i - m's map and counters are on the host: its buffers are free
+            if i - m >= first_timed:
                 segs[0] += int(host_stats[b][:wl.depth].sum())
         s = streams[b]
         with torch.cuda.stream(s):
@@ -512,7 +517,7 @@ def e2e_pipelined(step, wl, K, W, stream, world, rank):
         copied[b].record(copy)
 
     for i in range(W):
-        one(i, i % 2, W)
+        one(i, i % m, W)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -522,15 +527,16 @@ def e2e_pipelined(step, wl, K, W, stream, world, rank):
     for s in streams:
         s.wait_event(t0)
     for i in range(K):
-        one(W + i, (W + i) % 2, W)
+        one(W + i, (W + i) % m, W)
     t1.record(copy)
     torch.cuda.synchronize()
-    for j in (W + K - 2, W + K - 1):  # the last two steps' counters
+    for j in range(W + K - m, W + K):  # the last m steps' counters
         if j >= W:
-            segs[0] += int(host_stats[j % 2][:wl.depth].sum())
+            segs[0] += int(host_stats[j % m][:wl.depth].sum())
     ms = t0.elapsed_time(t1)
     n_segs = segs[0]
-    scenes[1].close()
+    for sc in scenes[1:]:
+        sc.close()
     if world > 1:
         import torch.distributed as dist
 
@@ -542,7 +548,7 @@ def e2e_pipelined(step, wl, K, W, stream, world, rank):
     return {"value": n_segs / (ms / 1e3), "unit": "rays/s", "h2d_bytes_per_step": int(wl.tris.nbytes),
             "d2h_bytes_per_step": int(step.tex.numel() * step.tex.element_size() + 8 * 16),
             "ms_per_step": ms / K,
-            "api": "two frames in flight on two streams and two resident scenes: splat_scene_update + "
+            "api": f"{m} frames in flight on {m} streams and {m} resident scenes: splat_scene_update + "
                    "splat_trace_forward + map/counter copies"}
 
 
