@@ -296,10 +296,12 @@ def run_ours(args):
     # the later bounces, so per-kernel event times there overlap.
     n_prof = min(K, 50)
     old_overlap = int(lib.splat_get_tuning(L.TUNE_SPLAT_OVERLAP))
+    old_split = int(lib.splat_get_tuning(L.TUNE_TRACE_SPLIT))
     kprof = C.c_void_p()
     L.check(lib.splat_profile_create(64 * (n_prof + 1), C.byref(kprof)))
     kstats = torch.zeros((n_prof, 16), dtype=torch.int64, device="cuda")
     L.check(lib.splat_set_tuning(L.TUNE_SPLAT_OVERLAP, 0))
+    L.check(lib.splat_set_tuning(L.TUNE_TRACE_SPLIT, 1))
     try:
         torch.cuda.synchronize()
         L.check(lib.splat_profile_attach(kprof))
@@ -310,6 +312,7 @@ def run_ours(args):
         L.check(lib.splat_profile_attach(None))
     finally:
         L.check(lib.splat_set_tuning(L.TUNE_SPLAT_OVERLAP, old_overlap))
+        L.check(lib.splat_set_tuning(L.TUNE_TRACE_SPLIT, old_split))
     kinds = {"generate": L.KERNEL_GENERATE, "hit_brute": L.KERNEL_HIT_BRUTE, "hit_bvh": L.KERNEL_HIT_BVH,
              "evolve": L.KERNEL_EVOLVE, "splat": L.KERNEL_SPLAT, "aux": L.KERNEL_AUX}
     prof_res = {}
@@ -357,7 +360,8 @@ def run_ours(args):
                 "peak_source": pk["source"], "algorithmic_bytes_per_launch": round(bytes_per_launch),
                 "avg_launch_ms": round(avg_launch_s * 1e3, 4),
                 "share": {k: round(v[1] / max(ms_all.value, 1e-12), 4) for k, v in prof_res.items()},
-                "kernel_times": f"{n_prof} separate steps with the splat overlap off (L2 flushed between steps)"}
+                "kernel_times": f"{n_prof} separate steps with the splat overlap off and one ray range "
+                                "(L2 flushed between steps)"}
     if dom == "hit_brute":
         # the brute-force hitter is FP32-issue bound: ray-triangle tests per
         # second against the issue peak at ~35 FP32 ops per hoisted test

@@ -498,7 +498,9 @@ enum {
                                             runs; 2 one splat per bounce on the side stream (default 2) */
     SPLAT_TUNE_BVH_REFILL = 7,           /* four-wide BVH, per-ray form: 0 a warp takes 32 new rays when all 32 are
                                             done; 1..32 a warp refills its finished lanes once that many are done */
-    SPLAT_TUNE_KEYS = 8
+    SPLAT_TUNE_TRACE_SPLIT = 8,          /* fused trace step: the rays as 1..4 independent ranges traced on
+                                            concurrent streams (steps of at least 2^17 rays; default 2) */
+    SPLAT_TUNE_KEYS = 9
 };
 splat_status_t splat_set_tuning(int32_t key, int32_t value);
 int32_t splat_get_tuning(int32_t key);

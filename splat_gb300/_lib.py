@@ -158,7 +158,8 @@ TUNE_SPLAT_AGGREGATE = 4
 TUNE_BVH_PACKET = 5
 TUNE_SPLAT_OVERLAP = 6
 TUNE_BVH_REFILL = 7
-TUNE_KEYS = 8
+TUNE_TRACE_SPLIT = 8
+TUNE_KEYS = 9
 
 KERNEL_GENERATE = 0
 KERNEL_HIT_BRUTE = 1

@@ -33,6 +33,7 @@ KNOB_CHOICES = {
     L.TUNE_BVH_PACKET: (0, 1, 2, 3, 4, 5),
     L.TUNE_SPLAT_OVERLAP: (0, 1, 2),
     L.TUNE_BVH_REFILL: (0, 16, 24),
+    L.TUNE_TRACE_SPLIT: (1, 2, 3),
 }
 
 

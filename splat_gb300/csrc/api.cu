@@ -711,17 +711,47 @@ splat_status_t splat_continuum_light_map(const splat_scene_t* scene, splat_adray
 // ---------------------------------------------------------------------------
 // fused trace step
 // ---------------------------------------------------------------------------
-size_t splat_trace_workspace_size(int64_t n_rays) { return n_rays <= 0 ? kAlign : work_bytes(n_rays); }
+
 
 // A side stream per (device, caller stream) of the calling host thread, with
 // fork / join events, for splats that run while later bounces trace.
 namespace {
 constexpr int kSideEvents = 10;
+constexpr int kMaxTraceParts = 4;
+constexpr int64_t kSplitMinRays = int64_t(1) << 17;  // smaller steps stay in one range
 struct SideStream {
     cudaStream_t s = nullptr;
     cudaEvent_t ev[kSideEvents] = {};
+    cudaStream_t part[kMaxTraceParts - 1] = {};   // streams of the concurrent ray ranges
+    cudaEvent_t part_ev[kMaxTraceParts] = {};     // fork, then one join per extra range
 };
+
+cudaError_t part_streams_ready(SideStream* x, int k) {
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < k; ++i)
+        if (!x->part[i] && (e = cudaStreamCreateWithFlags(&x->part[i], cudaStreamNonBlocking)) != cudaSuccess) return e;
+    for (int i = 0; i <= k; ++i)
+        if (!x->part_ev[i] && (e = cudaEventCreateWithFlags(&x->part_ev[i], cudaEventDisableTiming)) != cudaSuccess)
+            return e;
+    return cudaSuccess;
+}
+
+// Workspace of a step over cnt rays run as `parts` concurrent ranges.
+size_t trace_ws_bytes(int64_t cnt, int parts) {
+    return parts <= 1 ? work_bytes(cnt) : (size_t)parts * work_bytes((cnt + parts - 1) / parts);
+}
 }  // namespace
+
+// room for the step run as up to kMaxTraceParts concurrent ranges, plus the
+// statistics block splat_trace_forward_host keeps at the end
+constexpr size_t kHostStatsBytes = 256;
+
+size_t splat_trace_workspace_size(int64_t n_rays) {
+    if (n_rays <= 0) return kAlign;
+    size_t m = 0;
+    for (int p = 1; p <= kMaxTraceParts; ++p) m = std::max(m, trace_ws_bytes(n_rays, p));
+    return m + kHostStatsBytes;
+}
 
 // At most kSideStreams per host thread: a caller that cycles through many
 // short-lived streams gets the least recently used side stream destroyed
@@ -742,6 +772,10 @@ static cudaError_t side_stream_for(cudaStream_t caller, SideStream** out) {
         SideStream& old = lru->second.second;
         for (cudaEvent_t ev : old.ev)
             if (ev) cudaEventDestroy(ev);
+        for (cudaEvent_t ev : old.part_ev)
+            if (ev) cudaEventDestroy(ev);
+        for (cudaStream_t ps : old.part)
+            if (ps) cudaStreamDestroy(ps);
         if (old.s) cudaStreamDestroy(old.s);
         streams.erase(lru);
     }
@@ -761,36 +795,12 @@ static int64_t grid_rays(const splat_trace_params_t* P) {
     return (P->light.res1 / P->upscale) * (P->light.res2 / P->upscale);
 }
 
-splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace_params_t* P, void* d_map,
-                                   void* d_workspace, size_t workspace_bytes, splat_trace_stats_t* d_stats,
-                                   void* stream) {
-    if (!scene || !P) return fail(SPLAT_ERR_INVALID, "trace_forward: null scene or params");
-    if (!light_ok(&P->light, P->upscale)) return fail(SPLAT_ERR_INVALID, "trace_forward: bad light / upscale");
-    if (P->depth < 1 || P->depth > 8) return fail(SPLAT_ERR_INVALID, "trace_forward: depth must be 1..8");
-    if (!valid_material(&P->material)) return fail(SPLAT_ERR_INVALID, "trace_forward: bad material");
-    if (P->lambda_mode.mode == SPLAT_LAMBDA_STRATIFIED && P->lambda_mode.n_strata < 1)
-        return fail(SPLAT_ERR_INVALID, "trace_forward: n_strata < 1");
-    splat_status_t rc =
-        check_map(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
-    if (rc != SPLAT_OK) return rc;
-    if ((P->hitter == SPLAT_HITTER_BVH || P->hitter == SPLAT_HITTER_BVH2) && !scene->d_nodes && scene->n_recs > 0)
-        return fail(SPLAT_ERR_INVALID, "trace_forward: BVH hitter on a scene without BVH");
-    const int64_t n_grid = grid_rays(P);
-    const int64_t rb = P->ray_begin < 0 ? 0 : P->ray_begin;
-    const int64_t re = (P->ray_end <= 0 || P->ray_end > n_grid) ? n_grid : P->ray_end;
-    if (n_grid >= (int64_t(1) << 32)) return fail(SPLAT_ERR_INVALID, "trace_forward: more than 2^32 rays");
-    const int64_t cnt = re - rb;
-    if (cnt <= 0) return fail(SPLAT_ERR_INVALID, "trace_forward: empty ray range");
-    if (!d_workspace || workspace_bytes < work_bytes(cnt))
-        return fail(SPLAT_ERR_WORKSPACE, "trace_forward: workspace smaller than splat_trace_workspace_size");
-    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-    const int sm = sm_count_current();
-    Work w = carve_work(d_workspace, cnt);
-    SPLAT_CUDA(cudaMemsetAsync(w.counts, 0, kCounterBytes, st), "memset counters");
-    if (d_stats) SPLAT_CUDA(cudaMemsetAsync(d_stats, 0, sizeof(splat_trace_stats_t), st), "memset stats");
-    const int64_t planes = P->n_lambda > 0 ? P->n_lambda : 1;
-    if (P->zero_map) SPLAT_CUDA(cudaMemsetAsync(d_map, 0, (size_t)P->map_w * P->map_h * planes * 4, st), "clear map");
-
+// The forward step over rays [rb, rb + cnt) of the grid in the work area w,
+// on stream st: generate, depth x {hit, evolve (+ compaction, diffuse
+// queue)}, the splat (segments on a side stream), the statistics.  The map
+// and d_stats were cleared by the caller; statistics accumulate.
+static splat_status_t trace_part(const splat_scene_t* scene, const splat_trace_params_t* P, void* d_map, Work w,
+                                 int64_t rb, int64_t cnt, splat_trace_stats_t* d_stats, cudaStream_t st, int sm) {
     GenParams g;
     g.light = P->light;
     g.upscale = P->upscale;
@@ -824,6 +834,7 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
     const int overlap = P->depth > 1 ? g_tune[SPLAT_TUNE_SPLAT_OVERLAP] : 0;
     SideStream* side = nullptr;
     if (overlap) SPLAT_CUDA(side_stream_for(st, &side), "side stream");
+    splat_status_t rc = SPLAT_OK;
     int64_t* snap = &w.counts[kSplatSnap];
     int seg = 0, n_ev = 0;
     RaySoA cur = w.a, nxt = w.b;
@@ -845,7 +856,10 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
         }
         std::swap(cur, nxt);
         if (overlap && b < P->depth && (overlap == 2 || b == P->depth - 1)) {
-            SPLAT_CUDA(launch_copy_count(&w.counts[kSplatCount], &snap[b], st), "queue snapshot");
+            {
+                ProfScope ps(SPLAT_KERNEL_AUX, st);
+                SPLAT_CUDA(launch_copy_count(&w.counts[kSplatCount], &snap[b], st), "queue snapshot");
+            }
             SPLAT_CUDA(cudaEventRecord(side->ev[n_ev], st), "fork");
             SPLAT_CUDA(cudaStreamWaitEvent(side->s, side->ev[n_ev++], 0), "fork");
             ProfScope ps(SPLAT_KERNEL_SPLAT, side->s);
@@ -871,6 +885,68 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
     return SPLAT_OK;
 }
 
+
+splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace_params_t* P, void* d_map,
+                                   void* d_workspace, size_t workspace_bytes, splat_trace_stats_t* d_stats,
+                                   void* stream) {
+    if (!scene || !P) return fail(SPLAT_ERR_INVALID, "trace_forward: null scene or params");
+    if (!light_ok(&P->light, P->upscale)) return fail(SPLAT_ERR_INVALID, "trace_forward: bad light / upscale");
+    if (P->depth < 1 || P->depth > 8) return fail(SPLAT_ERR_INVALID, "trace_forward: depth must be 1..8");
+    if (!valid_material(&P->material)) return fail(SPLAT_ERR_INVALID, "trace_forward: bad material");
+    if (P->lambda_mode.mode == SPLAT_LAMBDA_STRATIFIED && P->lambda_mode.n_strata < 1)
+        return fail(SPLAT_ERR_INVALID, "trace_forward: n_strata < 1");
+    splat_status_t rc =
+        check_map(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
+    if (rc != SPLAT_OK) return rc;
+    if ((P->hitter == SPLAT_HITTER_BVH || P->hitter == SPLAT_HITTER_BVH2) && !scene->d_nodes && scene->n_recs > 0)
+        return fail(SPLAT_ERR_INVALID, "trace_forward: BVH hitter on a scene without BVH");
+    const int64_t n_grid = grid_rays(P);
+    const int64_t rb = P->ray_begin < 0 ? 0 : P->ray_begin;
+    const int64_t re = (P->ray_end <= 0 || P->ray_end > n_grid) ? n_grid : P->ray_end;
+    if (n_grid >= (int64_t(1) << 32)) return fail(SPLAT_ERR_INVALID, "trace_forward: more than 2^32 rays");
+    const int64_t cnt = re - rb;
+    if (cnt <= 0) return fail(SPLAT_ERR_INVALID, "trace_forward: empty ray range");
+    if (!d_workspace || workspace_bytes < work_bytes(cnt))
+        return fail(SPLAT_ERR_WORKSPACE, "trace_forward: workspace smaller than splat_trace_workspace_size");
+    // concurrent ray ranges (SPLAT_TUNE_TRACE_SPLIT), as many as the workspace holds
+    int parts = cnt >= kSplitMinRays ? g_tune[SPLAT_TUNE_TRACE_SPLIT] : 1;
+    while (parts > 1 && trace_ws_bytes(cnt, parts) > workspace_bytes) --parts;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const int sm = sm_count_current();
+    if (d_stats) SPLAT_CUDA(cudaMemsetAsync(d_stats, 0, sizeof(splat_trace_stats_t), st), "memset stats");
+    const int64_t planes = P->n_lambda > 0 ? P->n_lambda : 1;
+    if (P->zero_map) SPLAT_CUDA(cudaMemsetAsync(d_map, 0, (size_t)P->map_w * P->map_h * planes * 4, st), "clear map");
+    if (parts == 1) {
+        Work w = carve_work(d_workspace, cnt);
+        SPLAT_CUDA(cudaMemsetAsync(w.counts, 0, kCounterBytes, st), "memset counters");
+        return trace_part(scene, P, d_map, w, rb, cnt, d_stats, st, sm);
+    }
+    // the ranges are independent (ray ids are grid indices); each runs on its
+    // own stream after the clears above and joins the caller's stream
+    SideStream* side = nullptr;
+    SPLAT_CUDA(side_stream_for(st, &side), "part streams");
+    SPLAT_CUDA(part_streams_ready(side, parts - 1), "part streams");
+    SPLAT_CUDA(cudaEventRecord(side->part_ev[0], st), "fork ranges");
+    const int64_t each = (cnt + parts - 1) / parts;
+    const size_t region = work_bytes(each);
+    char* base = static_cast<char*>(d_workspace);
+    for (int i = 0; i < parts; ++i) {
+        const int64_t lo = rb + (int64_t)i * each;
+        const int64_t n_i = std::min(each, rb + cnt - lo);
+        cudaStream_t si = i == 0 ? st : side->part[i - 1];
+        if (i > 0) SPLAT_CUDA(cudaStreamWaitEvent(si, side->part_ev[0], 0), "fork ranges");
+        Work w = carve_work(base + (size_t)i * region, n_i);
+        SPLAT_CUDA(cudaMemsetAsync(w.counts, 0, kCounterBytes, si), "memset counters");
+        splat_status_t rc = trace_part(scene, P, d_map, w, lo, n_i, d_stats, si, sm);
+        if (rc != SPLAT_OK) return rc;
+    }
+    for (int i = 1; i < parts; ++i) {
+        SPLAT_CUDA(cudaEventRecord(side->part_ev[i], side->part[i - 1]), "join ranges");
+        SPLAT_CUDA(cudaStreamWaitEvent(st, side->part_ev[i], 0), "join ranges");
+    }
+    return SPLAT_OK;
+}
+
 splat_status_t splat_trace_forward_host(splat_scene_t* scene, const splat_ftri_t* host_tris,
                                         const splat_trace_params_t* P, void* host_map, void* d_map, void* d_workspace,
                                         size_t workspace_bytes, splat_trace_stats_t* host_stats, void* stream) {
@@ -883,22 +959,19 @@ splat_status_t splat_trace_forward_host(splat_scene_t* scene, const splat_ftri_t
         splat_status_t rc = scene_pack(scene, st);
         if (rc != SPLAT_OK) return rc;
     }
-    // stats live at the end of the workspace's counter block
-    splat_status_t rc = splat_trace_forward(scene, P, d_map, d_workspace, workspace_bytes, nullptr, stream);
+    // the statistics go to the last kHostStatsBytes of the workspace
+    if (workspace_bytes < kHostStatsBytes + kAlign)
+        return fail(SPLAT_ERR_WORKSPACE, "trace_forward_host: workspace smaller than splat_trace_workspace_size");
+    const size_t usable = (workspace_bytes - kHostStatsBytes) & ~size_t(15);
+    splat_trace_stats_t* d_stats = reinterpret_cast<splat_trace_stats_t*>(static_cast<char*>(d_workspace) + usable);
+    splat_status_t rc = splat_trace_forward(scene, P, d_map, d_workspace, usable, d_stats, stream);
     if (rc != SPLAT_OK) return rc;
     const int64_t planes = P->n_lambda > 0 ? P->n_lambda : 1;
     SPLAT_CUDA(cudaMemcpyAsync(host_map, d_map, (size_t)P->map_w * P->map_h * planes * 4, cudaMemcpyDeviceToHost, st),
                "download map");
-    if (host_stats) {
-        std::memset(host_stats, 0, sizeof(*host_stats));
-        const int64_t n_grid = grid_rays(P);
-        const int64_t rb = P->ray_begin < 0 ? 0 : P->ray_begin;
-        const int64_t re = (P->ray_end <= 0 || P->ray_end > n_grid) ? n_grid : P->ray_end;
-        Work w = carve_work(d_workspace, re - rb);
-        SPLAT_CUDA(cudaMemcpyAsync(host_stats->rays_per_bounce, w.counts, sizeof(int64_t) * (size_t)P->depth,
-                                   cudaMemcpyDeviceToHost, st),
-                   "download counters");
-    }
+    if (host_stats)
+        SPLAT_CUDA(cudaMemcpyAsync(host_stats, d_stats, sizeof(*host_stats), cudaMemcpyDeviceToHost, st),
+                   "download statistics");
     SPLAT_CUDA(cudaStreamSynchronize(st), "trace_forward_host sync");
     int32_t err = 0;
     SPLAT_CUDA(cudaMemcpy(&err, scene->d_err, sizeof(err), cudaMemcpyDeviceToHost), "read error word");
@@ -916,6 +989,8 @@ splat_status_t splat_set_tuning(int32_t key, int32_t value) {
         if (value < 0 || value > 2) return fail(SPLAT_ERR_INVALID, "set_tuning: splat overlap must be 0..2");
     } else if (key == SPLAT_TUNE_BVH_REFILL) {
         if (value < 0 || value > 32) return fail(SPLAT_ERR_INVALID, "set_tuning: refill threshold must be 0..32");
+    } else if (key == SPLAT_TUNE_TRACE_SPLIT) {
+        if (value < 1 || value > kMaxTraceParts) return fail(SPLAT_ERR_INVALID, "set_tuning: split must be 1..4");
     } else if (value < 1 || value > 256) {
         return fail(SPLAT_ERR_INVALID, "set_tuning: value must be 1..256");
     }

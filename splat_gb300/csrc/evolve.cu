@@ -458,10 +458,13 @@ cudaError_t launch_copy_count(const int64_t* src, int64_t* dst, cudaStream_t s) 
 
 __global__ void stats_finish_kernel(const int64_t* counts, int depth, const int64_t* splat_count,
                                     splat_trace_stats_t* st, const int32_t* err) {
+    // accumulates: a step run as several ray ranges adds each range's counts
+    // into statistics cleared once
     if (threadIdx.x == 0 && blockIdx.x == 0) {
-        for (int b = 0; b < 8; ++b) st->rays_per_bounce[b] = b < depth ? counts[b] : 0;
-        st->diffuse = splat_count ? *splat_count : st->diffuse;
-        st->error = err ? *err : 0;
+        for (int b = 0; b < depth && b < 8; ++b)
+            atomicAdd(reinterpret_cast<unsigned long long*>(&st->rays_per_bounce[b]), (unsigned long long)counts[b]);
+        if (splat_count) atomicAdd(reinterpret_cast<unsigned long long*>(&st->diffuse), (unsigned long long)*splat_count);
+        if (err) atomicOr(reinterpret_cast<unsigned long long*>(&st->error), (unsigned long long)(uint32_t)*err);
     }
 }
 

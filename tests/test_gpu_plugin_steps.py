@@ -145,3 +145,29 @@ def test_experimental_loop_composed_from_plugin_steps(torch_cuda, hitter, force_
     ig, ir = _sorted_rows(got), _sorted_rows(ref)
     assert_rays_equal(got[ig], ref[ir], "composed loop")
     assert np.array_equal(hit[ig], ref_hit[ir])
+
+
+def test_empty_inputs_are_no_ops(torch_cuda):
+    """Every plugin entry point accepts zero rays and leaves its outputs
+    alone; depth 0 run_evolution! only realigns the hits."""
+    from splat_gb300 import tracer
+
+    tris, fd = small_scene(2)
+    scene = tracer.Scene(tris, fd, bvh=True)
+    empty = torch_cuda.zeros(0, dtype=torch_cuda.uint8, device="cuda")
+    assert tracer.next_hit(scene, tracer.BVH, empty).numel() == 0
+    assert tracer.next_hit(scene, tracer.BRUTE, empty).numel() == 0
+    hit = torch_cuda.zeros(0, dtype=torch_cuda.int32, device="cuda")
+    tracer.evolve(scene, empty, hit, S.CAUCHY_GLASS, force_rand=0.5)
+    assert tracer.run_evolution(tracer.BVH, scene, empty, 3, S.CAUCHY_GLASS, 0.5).numel() == 0
+    tex = tracer.new_light_map(8, 8, 2, "i32")
+    tracer.continuum_light_map2(scene, empty, hit, S.stratified_spectrum(2), 1, tex)
+    assert int(tex.sum()) == 0
+    assert int(tracer.partition(empty).item()) == 0
+    rays = O.rays_from_light(S.hemisphere_light(1, 16, 1.05), 1, (T.LAMBDA_FIXED, 1, 550.0, 550.0), seed=2)
+    d = tracer.rays_to_device(rays)
+    h0 = tracer.run_evolution(tracer.BVH, scene, d, 0, S.CAUCHY_GLASS, 0.5)
+    o_hit, _ = O.next_hit(rays, tris)
+    assert np.array_equal(h0.cpu().numpy(), o_hit)
+    assert_rays_equal(tracer.rays_to_host(d), rays, "depth 0")
+    assert scene.errors() == 0

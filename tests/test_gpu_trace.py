@@ -215,3 +215,36 @@ def test_many_caller_streams(torch_cuda):
             outs.append(tracer.trace_forward(wl, scene=scene).tex)
     torch_cuda.cuda.synchronize()
     assert ref.sum() > 0 and all(torch_cuda.equal(o, ref) for o in outs)
+
+
+@pytest.mark.parametrize("accum", ["i32", "f32"])
+def test_ray_ranges_on_concurrent_streams(torch_cuda, accum):
+    """The fused step as 2, 3 and 4 ray ranges traced on concurrent streams
+    (SPLAT_TUNE_TRACE_SPLIT) against one range: int32 maps and statistics
+    identical, float maps within 1e-5 relative L1; the host entry point's
+    statistics (now accumulated on the device) match."""
+    from splat_gb300 import _lib as L
+    from splat_gb300 import tracer
+
+    lib = L.load()
+    old = lib.splat_get_tuning(L.TUNE_TRACE_SPLIT)
+    wl = S.realtime(light=S.scaled_light(S.realtime().light, 800), accum=accum)  # 160,000 rays, over 2^17
+    scene = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
+    try:
+        L.check(lib.splat_set_tuning(L.TUNE_TRACE_SPLIT, 1))
+        one, s1 = _gpu(wl, scene=scene)
+        for parts in (2, 3, 4):
+            L.check(lib.splat_set_tuning(L.TUNE_TRACE_SPLIT, parts))
+            got, sg = _gpu(wl, scene=scene)
+            assert sg == s1, (parts, sg, s1)
+            if accum == "i32":
+                assert np.array_equal(got, one), parts
+            else:
+                assert rel_l1(got, one) <= 1e-5
+            step = tracer.TraceStep(wl, scene)
+            host_map = np.zeros(got.shape, dtype=got.dtype)
+            st = step.run_host(np.ascontiguousarray(wl.tris), host_map)
+            assert st["rays_per_bounce"] == s1["rays_per_bounce"]
+    finally:
+        L.check(lib.splat_set_tuning(L.TUNE_TRACE_SPLIT, old))
+    assert one.sum() > 0
