@@ -91,13 +91,19 @@ class Batch:
     def replay(self, seeds: Optional[Sequence[int]] = None) -> None:
         import torch
 
+        gs = self.replay_async(seeds)
+        torch.cuda.current_stream().wait_stream(gs)
+
+    def replay_async(self, seeds: Optional[Sequence[int]] = None):
+        """Launches the captured graph on this engine's graph stream after the
+        current stream's work, without joining it back; returns the stream."""
         gs = self._graph_stream()
         if seeds:
             arr = (C.c_uint64 * len(seeds))(*[int(x) for x in seeds])
             L.check(L.load().splat_batch_replay(self._h, arr, len(seeds), gs.cuda_stream))
         else:
             L.check(L.load().splat_batch_replay(self._h, None, 0, gs.cuda_stream))
-        torch.cuda.current_stream().wait_stream(gs)
+        return gs
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None:
@@ -109,3 +115,40 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Lanes:
+    """Frames dealt to several batch engines ("lanes") whose captured graphs
+    replay concurrently, each on its own stream.  Frames go to the lane with
+    the fewest rays so far, largest first; one lane's latency-bound last
+    ticks then overlap the other lanes' work.  Every frame's map is still
+    the one it gets alone."""
+
+    def __init__(self, n_lanes: int, frames: Sequence, scenes: Sequence, maps: Sequence):
+        order = sorted(range(len(frames)), key=lambda i: -frames[i].n_rays)
+        load = [0] * n_lanes
+        self.members: List[List[int]] = [[] for _ in range(n_lanes)]
+        for i in order:
+            lane = min(range(n_lanes), key=lambda j: load[j])
+            self.members[lane].append(i)
+            load[lane] += frames[i].n_rays
+        self.engines = []
+        for lane in range(n_lanes):
+            idx = self.members[lane]
+            eng = Batch(max(1, len(idx)), max(1, sum(frames[i].n_rays for i in idx)) + 1024)
+            for i in idx:
+                eng.admit(scenes[i], frames[i], maps[i])
+            self.engines.append(eng)
+
+    def capture(self) -> int:
+        return max(e.capture() for e in self.engines)
+
+    def replay(self, seeds: Optional[Sequence[int]] = None) -> None:
+        """seeds: one per frame, in the order the frames were given."""
+        import torch
+
+        streams = [e.replay_async(None if seeds is None else [seeds[i] for i in idx])
+                   for e, idx in zip(self.engines, self.members)]
+        cur = torch.cuda.current_stream()
+        for gs in streams:
+            cur.wait_stream(gs)

@@ -139,3 +139,21 @@ def test_admission_respects_the_pool(frames):
     b.run()
     _check(wl, t1.cpu().numpy(), _alone(sc, wl), "first")
     _check(wl, t2.cpu().numpy(), _alone(sc, wl, 5), "second")
+
+
+def test_lanes_replay_concurrently_and_equal_alone(frames):
+    """Frames dealt to two engines whose graphs replay concurrently on two
+    streams: every map equals the frame's alone result, pass after pass."""
+    from splat_gb300 import batch, tracer
+
+    scenes = [sc for sc, _ in frames]
+    wls = [wl for _, wl in frames]
+    maps = [tracer.new_light_map(w.map_w, w.map_h, w.n_planes, w.accum) for w in wls]
+    lanes = batch.Lanes(2, wls, scenes, maps)
+    assert sorted(i for m in lanes.members for i in m) == list(range(len(wls)))
+    lanes.capture()
+    for k in range(2):
+        seeds = [w.seed + 7 * k for w in wls]
+        lanes.replay(seeds)
+        for i, (sc, wl) in enumerate(frames):
+            _check(wl, maps[i].cpu().numpy(), _alone(sc, wl, seeds[i]), f"frame {i} pass {k}")
