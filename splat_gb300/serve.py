@@ -95,15 +95,18 @@ class ScenePool:
 
 
 class Server:
-    """Continuous-batching renderer: the native server (splat_server_*: arrival
+    """Continuous-batching renderer: native servers (splat_server_*: arrival
     order, admission by engine slot, ray-pool room and light-map budget, one
     tick per step, bounded run-ahead, completion on the device) with scenes
-    kept resident by a ScenePool.  A request is handed to the native server
-    once it has arrived on the host clock, with its scene acquired; the scene
-    is released when the request completes."""
+    kept resident by a ScenePool.  A request is handed to a native server once
+    it has arrived on the host clock, with its scene acquired; the scene is
+    released when the request completes.  With lanes > 1 there is one native
+    server per lane, each stepping on its own stream; a request goes to the
+    lane with the fewest rays in flight, and one lane's latency-bound last
+    ticks overlap the others' work."""
 
     def __init__(self, scenes: ScenePool, budget_bytes: int, max_items: int = 128, max_pool_rays: int = 1 << 26,
-                 max_ticks_ahead: int = 4):
+                 max_ticks_ahead: int = 4, lanes: int = 2):
         import ctypes as C
 
         import torch
@@ -114,24 +117,29 @@ class Server:
         self.lib = L.load()
         self.scenes = scenes
         self.budget = int(budget_bytes)
-        self.engine_bytes = B.Batch.device_bytes(max_items, max_pool_rays)
-        self.max_items = int(max_items)
-        h = C.c_void_p()
-        L.check(self.lib.splat_server_create(int(max_items), int(max_pool_rays),
-                                             max(0, self.budget - self.engine_bytes), int(max_ticks_ahead),
-                                             C.byref(h)))
-        self.handle = h
-        self.stream = torch.cuda.current_stream()
+        n = max(1, int(lanes))
+        items, pool = max(1, int(max_items) // n), max(1, int(max_pool_rays) // n)
+        self.engine_bytes = n * B.Batch.device_bytes(items, pool)
+        self.max_items = items * n
+        map_budget = max(0, self.budget - self.engine_bytes) // n
+        self.handles, self.streams = [], []
+        for _ in range(n):
+            h = C.c_void_p()
+            L.check(self.lib.splat_server_create(items, pool, map_budget, int(max_ticks_ahead), C.byref(h)))
+            self.handles.append(h)
+            self.streams.append(torch.cuda.Stream())
+        self.lane_rays = [0] * n
         self.map_bytes_in_use = 0
-        self.inflight: Dict[int, Request] = {}   # native request id -> request
+        self.inflight: Dict[tuple, Request] = {}   # (lane, native request id) -> request
         self.pending: List[Request] = []
         self.done: List[Request] = []
         self._ids = (C.c_int64 * 256)()
         self._ms = (C.c_double * 256)()
-        # the server's device clock starts at its first step; the host clock
-        # is read right after it, with the stream idle
+        # each native server's device clock starts at its first step; the
+        # host clock is read right after them, with the streams idle
         torch.cuda.synchronize()
-        self._native_step()
+        for lane in range(n):
+            self._native_step(lane)
         torch.cuda.synchronize()
         self.host0 = time.perf_counter()
 
@@ -141,14 +149,15 @@ class Server:
     def submit(self, req: Request) -> None:
         heapq.heappush(self.pending, req)
 
-    def _native_step(self):
+    def _native_step(self, lane: int):
         C = self.C
         fl, q = C.c_int32(), C.c_int32()
-        self.L.check(self.lib.splat_server_step(self.handle, self.stream.cuda_stream, C.byref(fl), C.byref(q)))
+        self.L.check(self.lib.splat_server_step(self.handles[lane], self.streams[lane].cuda_stream, C.byref(fl),
+                                                C.byref(q)))
         return fl.value, q.value
 
     def _arrive(self) -> None:
-        """Hands every request that has arrived to the native server."""
+        """Hands every request that has arrived to the least loaded lane."""
         from . import tracer
 
         C = self.C
@@ -160,36 +169,43 @@ class Server:
             if sc is None:
                 return  # its scene fits only after requests in flight release theirs
             heapq.heappop(self.pending)
+            lane = min(range(len(self.handles)), key=lambda j: self.lane_rays[j])
             req.tex = tracer.new_light_map(req.wl.map_w, req.wl.map_h, req.wl.n_planes, req.wl.accum)
+            req.tex.record_stream(self.streams[lane])
+            self.streams[lane].wait_stream(self.torch.cuda.current_stream())  # the map's allocation
             P = tracer.trace_params(req.wl)
             rid = C.c_int64()
-            self.L.check(self.lib.splat_server_submit(self.handle, sc.handle, C.byref(P), req.tex.data_ptr(),
+            self.L.check(self.lib.splat_server_submit(self.handles[lane], sc.handle, C.byref(P), req.tex.data_ptr(),
                                                       C.byref(rid)))
-            self.inflight[int(rid.value)] = req
+            self.inflight[(lane, int(rid.value))] = req
+            self.lane_rays[lane] += req.wl.n_rays
             self.map_bytes_in_use += mb
 
     def step(self) -> int:
-        """Hands over what has arrived, enqueues one tick; returns the number
-        of requests completed so far."""
+        """Hands over what has arrived, enqueues one tick per lane; returns the
+        number of requests completed so far."""
         self._arrive()
-        self._native_step()
+        for lane in range(len(self.handles)):
+            self._native_step(lane)
         self._collect()
         return len(self.done)
 
     def _collect(self, block: bool = False) -> None:
         C = self.C
-        while True:
-            n = C.c_int32()
-            self.L.check(self.lib.splat_server_poll(self.handle, int(block), self._ids, self._ms, len(self._ids),
-                                                    C.byref(n)))
-            for i in range(n.value):
-                req = self.inflight.pop(int(self._ids[i]))
-                req.done_at = self._ms[i] / 1e3
-                self.scenes.release(req.scene_id)
-                self.map_bytes_in_use -= map_bytes(req.wl)
-                self.done.append(req)
-            if n.value < len(self._ids):
-                return
+        for lane, h in enumerate(self.handles):
+            while True:
+                n = C.c_int32()
+                self.L.check(self.lib.splat_server_poll(h, int(block), self._ids, self._ms, len(self._ids),
+                                                        C.byref(n)))
+                for i in range(n.value):
+                    req = self.inflight.pop((lane, int(self._ids[i])))
+                    req.done_at = self._ms[i] / 1e3
+                    self.scenes.release(req.scene_id)
+                    self.map_bytes_in_use -= map_bytes(req.wl)
+                    self.lane_rays[lane] -= req.wl.n_rays
+                    self.done.append(req)
+                if n.value < len(self._ids):
+                    break
 
     def drain(self) -> None:
         while self.pending or self.inflight:
@@ -201,14 +217,18 @@ class Server:
                     raise RuntimeError(f"request {self.pending[0].rid} can never fit the budget")
             self.step()
         self._collect(block=True)
+        cur = self.torch.cuda.current_stream()
+        for st in self.streams:
+            cur.wait_stream(st)
 
     def latencies(self) -> np.ndarray:
         return np.array([r.done_at - r.arrival for r in self.done])
 
     def close(self) -> None:
-        if getattr(self, "handle", None) is not None and self.handle.value:
-            self.lib.splat_server_destroy(self.handle)
-            self.handle = None
+        for h in getattr(self, "handles", []):
+            if h is not None and h.value:
+                self.lib.splat_server_destroy(h)
+        self.handles = []
 
     def __del__(self):
         try:
