@@ -10,7 +10,8 @@ from splat_gb300 import types as T
 pytestmark = pytest.mark.gpu
 
 
-def test_served_results_equal_alone():
+@pytest.mark.parametrize("split", [1 << 30, 1000], ids=["whole", "split"])
+def test_served_results_equal_alone(split):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
@@ -19,7 +20,7 @@ def test_served_results_equal_alone():
     scenes = {0: S.assemble(S.sphere_tris(3, noise_amp=0.05), S.floor_tris(-1.5, 4.0)),
               1: S.assemble(S.menger_tris(2, 2.0, rotation_seed=9), S.box_tris(3.0))}
     pool = serve.ScenePool(lambda sid: scenes[sid], 8 << 30)
-    srv = serve.Server(pool, 8 << 30, max_items=16, max_pool_rays=1 << 20)
+    srv = serve.Server(pool, 8 << 30, max_items=16, max_pool_rays=1 << 20, split_min_rays=split)
     rng = np.random.default_rng(3)
     for rid in range(24):
         sid = rid % 2
