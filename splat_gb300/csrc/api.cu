@@ -831,7 +831,7 @@ static splat_status_t trace_part(const splat_scene_t* scene, const splat_trace_p
     // side stream from a snapshot of the queue length, while the main stream
     // traces bounce b + 1.  Integer maps are sums, so the segmentation does
     // not change them; float maps change only in summation order.
-    const int overlap = P->depth > 1 ? g_tune[SPLAT_TUNE_SPLAT_OVERLAP] : 0;
+    const int overlap = P->depth > 1 ? g_tune[SPLAT_TUNE_SPLAT_OVERLAP].load() : 0;
     SideStream* side = nullptr;
     if (overlap) SPLAT_CUDA(side_stream_for(st, &side), "side stream");
     splat_status_t rc = SPLAT_OK;
@@ -909,7 +909,7 @@ splat_status_t splat_trace_forward(const splat_scene_t* scene, const splat_trace
     if (!d_workspace || workspace_bytes < work_bytes(cnt))
         return fail(SPLAT_ERR_WORKSPACE, "trace_forward: workspace smaller than splat_trace_workspace_size");
     // concurrent ray ranges (SPLAT_TUNE_TRACE_SPLIT), as many as the workspace holds
-    int parts = cnt >= kSplitMinRays ? g_tune[SPLAT_TUNE_TRACE_SPLIT] : 1;
+    int parts = cnt >= kSplitMinRays ? g_tune[SPLAT_TUNE_TRACE_SPLIT].load() : 1;
     while (parts > 1 && trace_ws_bytes(cnt, parts) > workspace_bytes) --parts;
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const int sm = sm_count_current();
@@ -998,7 +998,7 @@ splat_status_t splat_set_tuning(int32_t key, int32_t value) {
     return SPLAT_OK;
 }
 
-int32_t splat_get_tuning(int32_t key) { return key < 0 || key >= SPLAT_TUNE_KEYS ? -1 : g_tune[key]; }
+int32_t splat_get_tuning(int32_t key) { return key < 0 || key >= SPLAT_TUNE_KEYS ? -1 : g_tune[key].load(); }
 
 splat_status_t splat_profile_create(int32_t max_launches, splat_profile_t** out) {
     if (!out || max_launches < 1 || max_launches > (1 << 20)) return fail(SPLAT_ERR_INVALID, "profile_create: bad argument");

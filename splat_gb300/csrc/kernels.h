@@ -1,6 +1,7 @@
 // kernels.h -- host-side launchers shared by the translation units.
 #pragma once
 
+#include <atomic>
 #include <string>
 
 #include <cstdint>
@@ -13,7 +14,7 @@ namespace splat {
 // Kernels launched by this thread (for launch profiling).
 extern thread_local int64_t g_launches;
 // Launch-shape knobs, indexed by SPLAT_TUNE_*.
-extern int32_t g_tune[SPLAT_TUNE_KEYS];
+extern std::atomic<int32_t> g_tune[SPLAT_TUNE_KEYS];  // process-wide launch knobs (splat_set_tuning)
 
 // Where a hit kernel reads its rays: the structure-of-arrays bounce state
 // (count on the device) or the reference's AoS ADRay array.
