@@ -1,6 +1,9 @@
 """Shared test inputs and comparisons."""
 from __future__ import annotations
 
+import json
+import os
+
 import numpy as np
 
 from splat_gb300 import scenes as S
@@ -59,3 +62,28 @@ def rel_l1(a: np.ndarray, b: np.ndarray) -> float:
     a = a.astype(np.float64)
     b = b.astype(np.float64)
     return float(np.abs(a - b).sum() / max(np.abs(b).sum(), 1e-300))
+
+
+# The reference's own test vectors (tests/golden/make_golden.py).
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_tests.json"), encoding="utf-8"))
+
+
+def optics_scenario():
+    """The test/optics.jl ray and triangle as ADRay / FTri records."""
+    g = GOLDEN["optics_evolve"]
+    r = g["ray"]
+    rays = T.empty_rays(1)
+    rays["pos"][0], rays["dir"][0] = r["pos"], r["dir"]
+    rays["dp_dl"][0], rays["dd_dl"][0] = r["dp_dl"], r["dd_dl"]
+    rays["in_medium"][0] = 1 if r["in_medium"] else 0
+    rays["ignore_tri"][0], rays["dest"][0], rays["lam"][0] = r["ignore_tri"], r["dest"], r["lam"]
+    rays["status"][0] = {"ACTIVE": T.STATUS_ACTIVE, "DIFFUSE": T.STATUS_DIFFUSE, "INFINITY": T.STATUS_INFINITY}[r["status"]]
+    a, b, c = (np.asarray(g["tri_vertices"][k], np.float32) for k in ("a", "b", "c"))
+    n = np.cross(a - b, b - c).astype(np.float32)
+    n = (n * np.float32(1.0 / np.sqrt(np.float32(np.dot(n, n))))).astype(np.float32)
+    tri = np.zeros((1, 10, 3), np.float32)
+    tri[0, 0], tri[0, 1], tri[0, 2], tri[0, 3] = n, a, b, c
+    tri[0, 4] = tri[0, 5] = tri[0, 6] = n
+    hit = np.array([g["hit_index"]], np.int32)
+    rndm = np.array([g["rndm"]], np.float32)
+    return rays, tri, hit, rndm, g["first_diffuse"], (T.MATERIAL_LINEAR_REF, 0.0, 0.0)

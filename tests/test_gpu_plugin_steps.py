@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 from numpy.lib import recfunctions as rfn
 
-from helpers import assert_rays_equal, small_scene
+from helpers import assert_rays_equal, optics_scenario, small_scene
 from oracle import oracle as O
 from splat_gb300 import scenes as S
 from splat_gb300 import types as T
@@ -170,4 +170,20 @@ def test_empty_inputs_are_no_ops(torch_cuda):
     o_hit, _ = O.next_hit(rays, tris)
     assert np.array_equal(h0.cpu().numpy(), o_hit)
     assert_rays_equal(tracer.rays_to_host(d), rays, "depth 0")
+    assert scene.errors() == 0
+
+
+def test_evolve_reference_optics_scenario(torch_cuda):
+    """test/optics.jl:1-18 (evolve_ray(adr, 1, t, 1.0f0, 2) on the reference's
+    one ray and one triangle, from the committed fixture) through
+    splat_evolve: the ray and all its partials equal the oracle's."""
+    from splat_gb300 import tracer
+
+    rays, tris, hit, rndm, fd, mat = optics_scenario()
+    scene = tracer.Scene(tris, fd, bvh=False)
+    d = tracer.rays_to_device(rays)
+    tracer.evolve(scene, d, torch_cuda.from_numpy(hit).cuda(), mat, rndm=torch_cuda.from_numpy(rndm).cuda())
+    ref = O.evolve(rays, hit, tris, rndm, fd, mat)
+    assert_rays_equal(tracer.rays_to_host(d), ref, "optics.jl scenario")
+    assert ref[0]["status"] == T.STATUS_ACTIVE and not ref[0]["in_medium"]
     assert scene.errors() == 0

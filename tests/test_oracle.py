@@ -2,48 +2,91 @@
 
 * test/geo.jl:4-29 -- reflect axis cases, the regression golden vector
   (||reflect(d0, n) - d1|| < 1e-6) and distance_to_plane's sign symmetries
-  (the test file uses the stale name V3 for R3; restated with R3 semantics);
+  (the test file uses the stale name V3 for R3; restated with R3 semantics),
+  read from tests/golden/reference_tests.json;
+* test/optics.jl:1-18 -- the file's evolve_ray scenario, checked in
+  binary64 against the reference's refract;
 * src/atomic_argmin.jl:32-96 -- test_reversibility, test_comparison and
   test_comparison2 of the order-preserving float -> u32 map;
 * the published Philox4x32-10 known-answer vectors (Random123 kat_vectors);
 * structural facts of the reference's formulas (upres, glass, generator
   derivatives) and conservation laws of the trace step.
 """
+import os
+import sys
+
 import numpy as np
 import pytest
 
+from helpers import GOLDEN, optics_scenario
 from oracle import oracle as O
 from splat_gb300 import scenes as S
 from splat_gb300 import types as T
 
 # --------------------------------------------------------------- test/geo.jl
+# The reference's vectors come from tests/golden/reference_tests.json, which
+# tests/golden/make_golden.py extracts from its test files.
+GEO = GOLDEN["geo"]
 
 
-@pytest.mark.parametrize("v,n,want", [
-    ((-1, -1, 0), (0, 1, 0), (-1, 1, 0)),
-    ((-1, -1, 0), (0, -1, 0), (-1, 1, 0)),
-    ((-1, -1, 0), (1, 0, 0), (1, -1, 0)),
-    ((-1, -1, 0), (-1, 0, 0), (1, -1, 0)),
-    ((-4, -1, 0), (0, 1, 0), (-4, 1, 0)),
-    ((-1, -4, 0), (0, 1, 0), (-1, 4, 0)),
-])
-def test_reflect_axis_cases(v, n, want):
-    np.testing.assert_allclose(O.reflect(v, n), np.asarray(want, np.float32), rtol=0, atol=1e-6)
+@pytest.mark.parametrize("case", GEO["reflect_axis_cases"], ids=lambda c: f"{c['v']}|{c['n']}")
+def test_reflect_axis_cases(case):
+    np.testing.assert_allclose(O.reflect(case["v"], case["n"]), np.asarray(case["want"], np.float32), rtol=0,
+                               atol=1e-6)
 
 
 def test_reflect_regression_vector():
-    d0 = (-0.0993602, -0.990078, 0.0993602)
-    n = (0.21059, 0.310929, -0.926809)
-    d1 = np.asarray((0.077896, -0.728365, -0.680746), np.float32)
-    assert np.linalg.norm(O.reflect(d0, n) - d1) < 1e-6
+    g = GEO["reflect_regression"]
+    assert np.linalg.norm(O.reflect(g["d0"], g["n"]) - np.asarray(g["d1"], np.float32)) < g["tol"]
 
 
 def test_distance_to_plane_symmetries():
-    a = O.distance_to_plane((1, 2, 4), (2, 3, 1), (-2, 0, -2), (8, 1, 0))
+    dp = GEO["distance_to_plane"]
+    a, b = (O.distance_to_plane(c["o"], c["d"], c["p"], c["n"]) for c in dp["normal_sign_pair"])
     # the normal's sign does not matter (bit-equal)
-    assert a == O.distance_to_plane((1, 2, 4), (2, 3, 1), (-2, 0, -2), (-8, -1, 0))
+    assert a == b
     # a reversed direction gives the negated distance (bit-equal)
-    assert O.distance_to_plane((1, 2, 4), (-2, -3, -1), (-2, 0, -2), (8, 1, 0)) == -a
+    a, b = (O.distance_to_plane(c["o"], c["d"], c["p"], c["n"]) for c in dp["direction_sign_pair"])
+    assert a == -b
+
+
+def test_golden_fixture_matches_the_reference_test_files():
+    """The committed fixture is what make_golden.py reads from the
+    reference's test files (skipped where those files are absent)."""
+    root = os.environ.get("REFERENCE_ROOT", "/root/reference")
+    if not os.path.isfile(os.path.join(root, "test", "geo.jl")):
+        pytest.skip("reference test files not present")
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import make_golden
+
+    assert make_golden.generate(root) == GOLDEN
+
+
+def test_optics_scenario_follows_the_reference_refract():
+    """test/optics.jl:1-18: a ray inside glass (in_medium) at 550 nm along +x
+    from (-1, 0, 0) meets the triangle (1,1,1), (0,-2,1), (0,1,-2) with
+    draw 1.0 and first_diffuse 2.  The file asserts nothing; checked here in
+    binary64: the ray leaves at the plane hit (1/3, 0, 0), out of the
+    medium, along the reference's refract (src/geo.jl:548-561) with
+    n1 = glass(550), n2 = air.  That formula takes c1 = dot(v, n) against the
+    normal flipped toward the ray (c1 <= 0), where Snell's vector form takes
+    -dot; the direction differs from Snell's law and is kept as written."""
+    rays, tris, hit, rndm, fd, mat = optics_scenario()
+    out = O.evolve(rays, hit, tris, rndm, fd, mat)[0]
+    assert out["status"] == T.STATUS_ACTIVE and not out["in_medium"] and out["ignore_tri"] == 1
+    np.testing.assert_allclose(out["pos"], [1.0 / 3.0, 0.0, 0.0], atol=1e-6)
+    n = np.asarray(tris[0, 0], np.float64)
+    n /= np.linalg.norm(n)
+    v = np.asarray(rays[0]["dir"], np.float64)
+    if np.dot(v, n) > 0:
+        n = -n
+    c1 = np.dot(v / np.linalg.norm(v), n)
+    r = (1.3 + (1.4 - 1.3) / (700.0 - 400.0) * (550.0 - 400.0)) / 1.0  # glass(550) / air, src/material.jl:1-13
+    s2 = r * np.sqrt(1.0 - c1 * c1)
+    assert abs(s2) < 1.0  # can_refract
+    want = v * r + n * (r * c1 - np.sqrt(1.0 - s2 * s2))
+    want /= np.linalg.norm(want)
+    np.testing.assert_allclose(out["dir"], want, rtol=0, atol=2e-6)
 
 
 # ------------------------------------------------------ src/atomic_argmin.jl
