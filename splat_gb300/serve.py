@@ -104,10 +104,17 @@ class Server:
     server per lane, each stepping on its own stream; a request goes to the
     lane with the fewest rays in flight, or (split_min_rays set), from that
     many rays on, to every lane as disjoint ray ranges; one lane's
-    latency-bound last ticks overlap the others' work."""
+    latency-bound last ticks overlap the others' work.
+
+    A completed request is delivered: with on_done set, on_done(request) is
+    called once its map is complete on the device (the callback may copy
+    request.tex out or keep a reference), then the server drops its own
+    reference to the map, so a long-running server holds only the maps in
+    flight; without on_done, completed requests keep their maps in `done`."""
 
     def __init__(self, scenes: ScenePool, budget_bytes: int, max_items: int = 128, max_pool_rays: int = 1 << 26,
-                 max_ticks_ahead: int = 4, lanes: int = 2, split_min_rays: Optional[int] = None):
+                 max_ticks_ahead: int = 4, lanes: int = 2, split_min_rays: Optional[int] = None,
+                 on_done: Optional[Callable[[Request], None]] = None):
         import ctypes as C
 
         import torch
@@ -118,6 +125,7 @@ class Server:
         self.lib = L.load()
         self.scenes = scenes
         self.budget = int(budget_bytes)
+        self.on_done = on_done
         n = max(1, int(lanes))
         items, pool = max(1, int(max_items) // n), max(1, int(max_pool_rays) // n)
         self.engine_bytes = n * B.Batch.device_bytes(items, pool)
@@ -222,6 +230,9 @@ class Server:
                     req.done_at = left[1]
                     self.scenes.release(req.scene_id)
                     self.map_bytes_in_use -= map_bytes(req.wl)
+                    if self.on_done is not None:
+                        self.on_done(req)
+                        req.tex = None
                     self.done.append(req)
                 if n.value < len(self._ids):
                     break

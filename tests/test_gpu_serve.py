@@ -45,6 +45,41 @@ def test_served_results_equal_alone(split):
         assert torch.equal(r.tex, alone), f"request {r.rid} differs from its alone result"
 
 
+def test_served_maps_delivered_then_released():
+    """With on_done, each completed request is delivered once (here: its map
+    copied to the host), the server keeps no map of its own afterwards, and
+    every delivered map equals the frame rendered alone."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from splat_gb300 import serve, tracer
+
+    scenes = {0: S.assemble(S.sphere_tris(3, noise_amp=0.05), S.floor_tris(-1.5, 4.0))}
+    pool = serve.ScenePool(lambda sid: scenes[sid], 8 << 30)
+    delivered = {}
+
+    def deliver(req):
+        assert req.rid not in delivered
+        delivered[req.rid] = req.tex.cpu()
+
+    srv = serve.Server(pool, 8 << 30, max_items=16, max_pool_rays=1 << 20, on_done=deliver)
+    tris, fd = scenes[0]
+    wls = []
+    for rid in range(12):
+        wl = S.Workload(name=f"d{rid}", tris=tris, first_diffuse=fd, light=S.hemisphere_light(rid, 64 + 8 * rid, 1.1),
+                        depth=3, spectrum=S.stratified_spectrum(4), lambda_mode=(T.LAMBDA_STRATIFIED, 4, 400.0, 700.0),
+                        material=S.CAUCHY_GLASS, map_w=96, map_h=64, accum="i32", hitter="bvh", seed=900 + rid)
+        wls.append(wl)
+        srv.submit(serve.Request(arrival=0.001 * rid, rid=rid, scene_id=0, wl=wl))
+    srv.drain()
+    assert sorted(delivered) == list(range(12))
+    assert len(srv.done) == 12 and all(r.tex is None for r in srv.done)
+    assert srv.map_bytes_in_use == 0
+    for rid, wl in enumerate(wls):
+        alone = tracer.trace_forward(wl, scene=pool.resident[0]).tex.cpu()
+        assert torch.equal(delivered[rid], alone), f"request {rid} differs from its alone result"
+
+
 def test_native_server_budget_and_order():
     """splat_server_* directly: with a map budget that holds one request's map
     at a time, requests still complete, one after another, in arrival order,
