@@ -772,7 +772,7 @@ def run_served(args):
 
     # continuous batching; a completed map is delivered (here: dropped, as the
     # plain loop below drops its maps) and the server keeps only maps in flight
-    srv = serve.Server(pool, budget, max_items=128, max_pool_rays=1 << 26, on_done=lambda req: None)
+    srv = serve.Server(pool, budget, max_items=128, on_done=lambda req: None)
     for t, sid, wl in reqs:
         srv.submit(serve.Request(arrival=t + 0.5, rid=len(srv.pending), scene_id=sid, wl=wl))
     srv.drain()
@@ -817,7 +817,7 @@ def run_served(args):
 
     # capacity: the same requests all queued at once, device time to finish them
     sub = reqs[: min(len(reqs), 400)]
-    srv = serve.Server(pool, budget, max_items=128, max_pool_rays=1 << 26, on_done=lambda req: None)
+    srv = serve.Server(pool, budget, max_items=128, on_done=lambda req: None)
     for t, sid, wl in sub:
         srv.submit(serve.Request(arrival=0.0, rid=len(srv.pending), scene_id=sid, wl=wl))
     srv.drain()
@@ -856,7 +856,8 @@ def run_served(args):
            "config": {"workload": f"Poisson {args.rate} req/s for {args.duration} s, 32-scene pool (Menger level 3, "
                                   f"96,012 tris), per-request rays log-uniform [2^14, 2^22], depth 2-6, 1-16 planes, "
                                   f"maps 256^2-2048^2 int32, light within 5 degrees",
-                      "hbm_budget_gb": 150, "scene_loads": pool.loads, "scene_evictions": pool.evictions},
+                      "hbm_budget_gb": 150, "scene_loads": pool.loads, "scene_evictions": pool.evictions,
+                      "server": "2 lanes, 128 request slots, 2^24 rays in flight"},
            "served": served, "plain_per_frame_loop": plain,
            "capacity_frames_per_s": {"served": cap_served, "plain_per_frame_loop": cap_plain,
                                      "dropin_per_frame_loop": cap_dropin,

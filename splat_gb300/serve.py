@@ -110,9 +110,18 @@ class Server:
     called once its map is complete on the device (the callback may copy
     request.tex out or keep a reference), then the server drops its own
     reference to the map, so a long-running server holds only the maps in
-    flight; without on_done, completed requests keep their maps in `done`."""
+    flight; without on_done, completed requests keep their maps in `done`.
 
-    def __init__(self, scenes: ScenePool, budget_bytes: int, max_items: int = 128, max_pool_rays: int = 1 << 26,
+    max_pool_rays bounds the rays in flight (split evenly over the lanes).
+    Every tick advances all of a lane's requests by one bounce, so a tick
+    lasts about as long as its lane's rays take; the bound keeps a burst of
+    arrivals from stretching every tick (and every request's latency) and
+    leaves the excess queued in arrival order.  Each lane must hold the
+    largest request.  Measured on Poisson Menger requests of up to 2^22
+    rays at 400 req/s: p99 244 ms with 2^26 rays in flight, 38 ms with 2^24
+    (the default), p50 5.6 -> 5.1 ms; at 200 req/s no change."""
+
+    def __init__(self, scenes: ScenePool, budget_bytes: int, max_items: int = 128, max_pool_rays: int = 1 << 24,
                  max_ticks_ahead: int = 4, lanes: int = 2, split_min_rays: Optional[int] = None,
                  on_done: Optional[Callable[[Request], None]] = None):
         import ctypes as C
