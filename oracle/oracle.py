@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
-by bench.py's cpu_baseline / reference leg, always as the checker or as the
+by bench.py's cpu_baseline / reference leg, always as the correctness reference or as the
 timed CPU baseline, never as part of the product path.
 """
 from __future__ import annotations
