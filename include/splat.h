@@ -237,7 +237,10 @@ splat_status_t splat_next_hit_brute(const splat_adray_t* d_rays, int64_t n_rays,
  *   - n_rays above SPLAT_STATIC_HIT_MAX_RAYS is rejected (SPLAT_ERR_INVALID);
  *   - the first call on a device looks the array's device address up (once
  *     per device, with that device current); make that first call before
- *     any stream capture;
+ *     any stream capture.  The address is kept for the life of the process:
+ *     after cudaDeviceReset (or any teardown of the device's primary
+ *     context) it is stale, so do not call this entry point again on that
+ *     device after a reset;
  *   - every call shares the array and first resets the words it uses, so
  *     calls whose kernels overlap on the GPU (other streams, other host
  *     threads) race and must be serialised by the caller;

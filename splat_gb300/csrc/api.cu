@@ -1,4 +1,5 @@
 // api.cu -- the extern "C" entry points of libsplat (include/splat.h).
+#include <atomic>
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -37,13 +38,17 @@ splat_status_t cuda_fail(cudaError_t e, const char* what) {
     } while (0)
 
 int sm_count_current() {
-    static int cache[64] = {0};
+    // read from any host thread: each device's count is written once
+    static std::atomic<int> cache[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 152;
-    if (dev >= 0 && dev < 64 && cache[dev]) return cache[dev];
+    if (dev >= 0 && dev < 64) {
+        int c = cache[dev].load(std::memory_order_relaxed);
+        if (c) return c;
+    }
     int n = 152;
     cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (dev >= 0 && dev < 64) cache[dev] = n;
+    if (dev >= 0 && dev < 64) cache[dev].store(n, std::memory_order_relaxed);
     return n;
 }
 

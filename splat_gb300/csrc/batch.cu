@@ -5,7 +5,8 @@
 // structure-of-arrays pool whose ray ids carry the item slot (slot << 24 |
 // local ray index).  One tick advances every in-flight item by one bounce:
 //
-//   reserve   one thread appends the rays of items starting this tick after
+//   reserve   one thread per item slot; block scans over the slots give
+//             each item starting this tick its offset in the ray pool, after
 //             the survivors of the previous tick
 //   generate  rays_from_light of those items (src/ray_generators.jl:64-97)
 //   hit       per ray, its item's four-wide BVH or a per-ray brute loop

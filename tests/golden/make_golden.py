@@ -13,7 +13,8 @@ ADRay (pos, dpos/dλ, dir, ddir/dλ, in_medium, ignore_tri, dest, λ, status);
 the fixture records the values, not the constructors.
 
 Usage: python tests/golden/make_golden.py [reference root]
-(default: the REFERENCE_ROOT environment variable, else /root/reference).
+(the reference checkout: the argument, else the REFERENCE_ROOT environment
+variable; one of them is required).
 """
 from __future__ import annotations
 
@@ -85,7 +86,9 @@ def generate(root: str) -> dict:
 
 
 def main() -> None:
-    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE_ROOT", "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <reference root> (or set REFERENCE_ROOT)")
     data = generate(root)
     with open(OUT, "w", encoding="utf-8") as f:
         json.dump(data, f, indent=1)

@@ -57,10 +57,12 @@ def test_malformed_files_fail_cleanly(tmp_path, body, what):
         S.load_obj(str(tmp_path / "missing.obj"))
 
 
-REF_ICOS = "/root/reference/objs/icos.obj"
+# the reference checkout, when the environment names one (REFERENCE_ROOT)
+REF_ICOS = os.path.join(os.environ.get("REFERENCE_ROOT", ""), "objs", "icos.obj")
 
 
-@pytest.mark.skipif(not os.path.exists(REF_ICOS), reason="reference assets not present")
+@pytest.mark.skipif(not os.environ.get("REFERENCE_ROOT") or not os.path.exists(REF_ICOS),
+                    reason="REFERENCE_ROOT unset or without objs/icos.obj")
 def test_reference_icosphere_asset_loads():
     """The reference's own smoke-test asset (objs/icos.obj, subdivision-3
     icosphere): 1280 triangles, unit vertex normals, outward plane normals."""

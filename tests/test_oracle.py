@@ -53,9 +53,9 @@ def test_distance_to_plane_symmetries():
 def test_golden_fixture_matches_the_reference_test_files():
     """The committed fixture is what make_golden.py reads from the
     reference's test files (skipped where those files are absent)."""
-    root = os.environ.get("REFERENCE_ROOT", "/root/reference")
-    if not os.path.isfile(os.path.join(root, "test", "geo.jl")):
-        pytest.skip("reference test files not present")
+    root = os.environ.get("REFERENCE_ROOT")
+    if not root or not os.path.isfile(os.path.join(root, "test", "geo.jl")):
+        pytest.skip("REFERENCE_ROOT unset or without test/geo.jl")
     sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
     import make_golden
 

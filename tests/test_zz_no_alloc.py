@@ -8,6 +8,8 @@ point that takes caller scratch), exactly, on two calls in a row; the second
 call is smaller, so stale words from the first call would show.  Collected
 last so that a failure here comes after every other test has run."""
 import ctypes as C
+import os
+import re
 
 import numpy as np
 import pytest
@@ -40,7 +42,15 @@ def test_static_scratch_hitter_matches_the_allocating_one():
         assert np.array_equal(got, ref), f"call {call}: {np.nonzero(got != ref)[0][:10]}"
         assert (ref > 1).sum() > n // 4
 
-    # sizes beyond the library's scratch are refused with a clear message
+    # the Python constant is the header's cap
+    header = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include",
+                               "splat.h")).read()
+    cap = re.search(r"#define SPLAT_STATIC_HIT_MAX_RAYS \(1 << (\d+)\)", header)
+    assert cap and (1 << int(cap.group(1))) == L.STATIC_HIT_MAX_RAYS
+
+    # sizes beyond the library's scratch are refused with a clear message;
+    # the size check comes before any launch, so the short hit buffer of the
+    # last call above is never written
     too_many = L.STATIC_HIT_MAX_RAYS + 1
     rc = lib.splat_next_hit_brute_static(d_rays.data_ptr(), too_many, d_nt.data_ptr(), nt, hit.data_ptr(), stream)
     assert rc == L.ERR_INVALID
