@@ -503,7 +503,15 @@ enum {
                                             done; 1..32 a warp refills its finished lanes once that many are done */
     SPLAT_TUNE_TRACE_SPLIT = 8,          /* fused trace step: the rays as 1..4 independent ranges traced on
                                             concurrent streams (steps of at least 2^17 rays; default 2) */
-    SPLAT_TUNE_KEYS = 9
+    SPLAT_TUNE_TEST_WAIT_STALL = 9,      /* test only (default 0, off): k > 0 makes the brute-force hitter's wait for
+                                            tile k - 1 of every block poll a barrier that nothing completes (64
+                                            polls), so each block takes the failure path of its bounded waits:
+                                            error bit 1, bounded drain of its copies in flight, early return */
+    SPLAT_TUNE_RAY_ORDER = 10,           /* fused trace step, four-wide BVH: 0 secondary rays traced in compaction
+                                            order; 4..20 each bounce after the first groups its rays by (direction
+                                            octant, BVH position of the triangle they leave), a key of that many
+                                            bits, before the hit launch (default 0) */
+    SPLAT_TUNE_KEYS = 11
 };
 splat_status_t splat_set_tuning(int32_t key, int32_t value);
 int32_t splat_get_tuning(int32_t key);

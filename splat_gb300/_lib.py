@@ -159,7 +159,9 @@ TUNE_BVH_PACKET = 5
 TUNE_SPLAT_OVERLAP = 6
 TUNE_BVH_REFILL = 7
 TUNE_TRACE_SPLIT = 8
-TUNE_KEYS = 9
+TUNE_TEST_WAIT_STALL = 9
+TUNE_RAY_ORDER = 10
+TUNE_KEYS = 11
 
 KERNEL_GENERATE = 0
 KERNEL_HIT_BRUTE = 1

@@ -80,6 +80,7 @@ struct Work {
     int32_t* hit;
     uint64_t* tmp;
     int64_t* counts;  // counts[b] = active rays after bounce b (b <= 64); counts[kSplatCount] = queued
+    void* order;      // ray-order sort scratch (ray_order_bytes(cap))
 };
 constexpr int kSplatCount = 96;
 constexpr int kSplatSnap = 100;  // counts[kSplatSnap + b]: splat queue length after bounce b (b <= 8)
@@ -87,7 +88,8 @@ constexpr int kFetchBase = 128;  // counts[kFetchBase + b]: work counter of boun
 constexpr size_t kCounterBytes = 2048;
 
 size_t work_bytes(int64_t cap) {
-    return 3 * soa_bytes(cap) + align_up(4 * (size_t)cap) + align_up(8 * (size_t)cap) + kCounterBytes + kAlign;
+    return 3 * soa_bytes(cap) + align_up(4 * (size_t)cap) + align_up(8 * (size_t)cap) + kCounterBytes +
+           align_up(ray_order_bytes(cap)) + kAlign;
 }
 
 Work carve_work(void* ws, int64_t cap) {
@@ -101,6 +103,8 @@ Work carve_work(void* ws, int64_t cap) {
     w.tmp = reinterpret_cast<uint64_t*>(p);
     p += align_up(8 * (size_t)cap);
     w.counts = reinterpret_cast<int64_t*>(p);
+    p += kCounterBytes;
+    w.order = p;
     return w;
 }
 
@@ -176,6 +180,7 @@ struct splat_scene {
     int64_t n_nodes = 0;
     TriHit* d_bvh = nullptr;
     int32_t* d_order = nullptr;
+    int32_t* d_bvh_pos = nullptr;  // inverse of d_order (n_tris + 1 entries, by reference index)
     int32_t* d_links = nullptr;  // refit links of the two-child tree
     Bvh4Node* d_nodes4 = nullptr;
     int64_t n_nodes4 = 0;
@@ -204,6 +209,7 @@ static void scene_free(splat_scene* s) {
     cudaFree(s->d_nodes);
     cudaFree(s->d_bvh);
     cudaFree(s->d_order);
+    cudaFree(s->d_bvh_pos);
     cudaFree(s->d_links);
     cudaFree(s->d_nodes4);
     cudaFree(s->d_links4);
@@ -222,7 +228,7 @@ static cudaError_t dalloc(T** p, size_t bytes, int64_t& total) {
 static splat_status_t scene_pack(splat_scene* s, cudaStream_t st) {
     ProfScope ps(SPLAT_KERNEL_AUX, st);
     cudaError_t e = launch_pack_hits(s->d_ftri, s->n_tris, s->d_brute, s->d_boxes, s->d_scale, s->d_order, s->d_bvh,
-                                     st);
+                                     s->d_bvh_pos, st);
     if (e != cudaSuccess) return cuda_fail(e, "pack hit records");
     if (s->d_nodes && s->d_links) {
         e = launch_refit_tree(s->d_nodes, false, s->n_nodes, s->d_links, s->d_flags, s->d_bvh, s->d_ftri, s->d_scale,
@@ -306,6 +312,7 @@ splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris,
         chk(dalloc(&s->d_nodes, sizeof(BvhNode) * bvh.nodes.size(), s->bytes));
         chk(dalloc(&s->d_bvh, sizeof(TriHit) * (size_t)s->n_recs, s->bytes));
         chk(dalloc(&s->d_order, sizeof(int32_t) * bvh.order.size(), s->bytes));
+        chk(dalloc(&s->d_bvh_pos, sizeof(int32_t) * ((size_t)n_tris + 1), s->bytes));
         chk(dalloc(&s->d_links, sizeof(int32_t) * bvh.links.size(), s->bytes));
         s->n_nodes4 = (int64_t)bvh.nodes4.size();
         s->cap_nodes = s->n_nodes;
@@ -338,7 +345,8 @@ splat_status_t splat_scene_create(const splat_ftri_t* host_tris, int64_t n_tris,
                             cudaMemcpyHostToDevice, st));
     }
     if (e == cudaSuccess)
-        chk(launch_pack_hits(s->d_ftri, n_tris, s->d_brute, s->d_boxes, s->d_scale, s->d_order, s->d_bvh, st));
+        chk(launch_pack_hits(s->d_ftri, n_tris, s->d_brute, s->d_boxes, s->d_scale, s->d_order, s->d_bvh,
+                             s->d_bvh_pos, st));
     // host vectors above must outlive the async copies
     if (e == cudaSuccess) chk(cudaStreamSynchronize(st));
     if (e != cudaSuccess) {
@@ -413,6 +421,10 @@ static splat_status_t scene_rebuild_gpu(splat_scene* s, cudaStream_t st) {
         int64_t cap = 0;
         SPLAT_CUDA(grow(&s->d_order, cap, np, sizeof(int32_t)), "scene_rebuild: order");
     }
+    if (!s->d_bvh_pos) {
+        int64_t cap = 0;
+        SPLAT_CUDA(grow(&s->d_bvh_pos, cap, s->n_tris + 1, sizeof(int32_t)), "scene_rebuild: order inverse");
+    }
     if (!s->d_lbvh) {
         const size_t b = lbvh_scratch_bytes(np);
         SPLAT_CUDA(cudaMalloc(&s->d_lbvh, b), "scene_rebuild: scratch");
@@ -421,7 +433,8 @@ static splat_status_t scene_rebuild_gpu(splat_scene* s, cudaStream_t st) {
     SPLAT_CUDA(launch_lbvh_build(s->d_ftri, s->n_tris, kLbvhLeaf, s->d_lbvh, s->d_nodes, s->d_nodes4, s->d_order,
                                  sm_count_current(), st),
                "scene_rebuild: build");
-    SPLAT_CUDA(launch_pack_hits(s->d_ftri, s->n_tris, s->d_brute, s->d_boxes, s->d_scale, s->d_order, s->d_bvh, st),
+    SPLAT_CUDA(launch_pack_hits(s->d_ftri, s->n_tris, s->d_brute, s->d_boxes, s->d_scale, s->d_order, s->d_bvh,
+                                s->d_bvh_pos, st),
                "scene_rebuild: pack");
     s->gpu_bvh = true;
     s->n_nodes = need;
@@ -843,9 +856,17 @@ static splat_status_t trace_part(const splat_scene_t* scene, const splat_trace_p
     int64_t* snap = &w.counts[kSplatSnap];
     int seg = 0, n_ev = 0;
     RaySoA cur = w.a, nxt = w.b;
+    const int order_bits = g_tune[SPLAT_TUNE_RAY_ORDER].load();
     for (int32_t b = 1; b <= P->depth; ++b) {
         RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0,
                    reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b]), packet_for(b)};
+        if (b >= 2 && order_bits > 0 && P->hitter == SPLAT_HITTER_BVH && scene->d_nodes4 && scene->d_bvh_pos) {
+            // secondary rays in coherent order: (octant, position of the triangle they leave)
+            ProfScope ps(SPLAT_KERNEL_AUX, st);
+            SPLAT_CUDA(launch_ray_order(cur.f, cur.ignore, cur.cap, &w.counts[b - 1], scene->d_bvh_pos,
+                                        scene->n_tris, order_bits, w.order, &src.perm, sm, st),
+                       "ray order");
+        }
         rc = hit_any(scene, P->hitter, src, cnt, w.hit, nullptr, w.tmp, st);
         if (rc != SPLAT_OK) return rc;
         ea.in = cur;
@@ -996,6 +1017,11 @@ splat_status_t splat_set_tuning(int32_t key, int32_t value) {
         if (value < 0 || value > 32) return fail(SPLAT_ERR_INVALID, "set_tuning: refill threshold must be 0..32");
     } else if (key == SPLAT_TUNE_TRACE_SPLIT) {
         if (value < 1 || value > kMaxTraceParts) return fail(SPLAT_ERR_INVALID, "set_tuning: split must be 1..4");
+    } else if (key == SPLAT_TUNE_RAY_ORDER) {
+        if (value != 0 && (value < 4 || value > 20))
+            return fail(SPLAT_ERR_INVALID, "set_tuning: ray order bits must be 0 or 4..20");
+    } else if (key == SPLAT_TUNE_TEST_WAIT_STALL) {
+        if (value < 0 || value > (1 << 20)) return fail(SPLAT_ERR_INVALID, "set_tuning: stall tile must be 0..2^20");
     } else if (value < 1 || value > 256) {
         return fail(SPLAT_ERR_INVALID, "set_tuning: value must be 1..256");
     }
@@ -1835,7 +1861,7 @@ splat_status_t splat_render_camera_after(const splat_scene_t* scene, const splat
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
     const int sm = sm_count_current();
     Work w = carve_work(d_workspace, cnt);
-    char* p = reinterpret_cast<char*>(w.counts) + kCounterBytes;
+    char* p = static_cast<char*>(w.order) + align_up(ray_order_bytes(cnt));
     p = reinterpret_cast<char*>(align_up(reinterpret_cast<size_t>(p)));
     const RaySoA sky = carve_soa(p, cnt);
     int64_t* sky_count = &w.counts[kSplatCount + 1];

@@ -24,7 +24,7 @@
 namespace splat {
 
 thread_local int64_t g_launches = 0;
-std::atomic<int32_t> g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1, 2, 0, 2};
+std::atomic<int32_t> g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1, 2, 0, 2, 0, 0};
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + bulk copy (sm_90+ async proxy)
@@ -61,11 +61,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
 // Bounded wait: gives up after kWaitLimit polls (each poll may suspend the
 // thread for a hardware-chosen time), so a lost copy cannot hang the GPU.
 constexpr uint32_t kWaitLimit = 1u << 24;
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase) {
-    for (uint32_t it = 0; it < kWaitLimit; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t phase, uint32_t limit = kWaitLimit) {
+    for (uint32_t it = 0; it < limit; ++it)
         if (mbar_try_wait(bar, phase)) return true;
     return false;
 }
+// Polls of the stalled wait that SPLAT_TUNE_TEST_WAIT_STALL injects.
+constexpr uint32_t kStallPolls = 64;
 
 // ---------------------------------------------------------------------------
 // brute force, TMA-staged tiles
@@ -81,11 +83,15 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
                                                                   int32_t* __restrict__ hit_idx,
                                                                   float* __restrict__ hit_t,
                                                                   unsigned long long* __restrict__ tmp,
-                                                                  int32_t* err) {
+                                                                  int32_t* err, int stall_tile) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TriHit* tiles = reinterpret_cast<TriHit*>(smem_raw);
     TriBox* btiles = reinterpret_cast<TriBox*>(smem_raw + (size_t)kStages * kTile * sizeof(TriHit));
     __shared__ __align__(8) uint64_t bars[kStages];
+    // stall_tile >= 0 (test only): the wait for that tile polls `stall`, a
+    // barrier that no copy and no thread ever completes, kStallPolls times,
+    // so the block takes the failure path below with its copies in flight
+    __shared__ __align__(8) uint64_t stall;
 
     const int64_t n = src.d_count ? *src.d_count : src.n;
     const int64_t ray0 = (int64_t)blockIdx.x * kBruteThreads * RPT;
@@ -119,6 +125,7 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+        mbar_init(&stall, 1);
         fence_mbar_init();
     }
     __syncthreads();
@@ -141,7 +148,7 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
     for (int kt = 0; kt < n_tiles; ++kt) {
         const int s = kt % kStages;
         const uint32_t ph = (uint32_t)(kt / kStages) & 1u;
-        const bool ok = mbar_wait_bounded(&bars[s], ph);
+        const bool ok = kt == stall_tile ? mbar_wait_bounded(&stall, 0u, kStallPolls) : mbar_wait_bounded(&bars[s], ph);
         if (__syncthreads_or(!ok)) {
             failed = true;
             break;
@@ -185,7 +192,8 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
     if (failed) {
         if (threadIdx.x == 0) {
             atomicOr(err, 1);
-            // drain this block's copies still in flight (bounded) before exit
+            // drain this block's copies still in flight (bounded) before exit:
+            // tiles consumed .. consumed + kStages - 1 were issued
             const int issued = min(n_tiles, consumed + kStages);
             for (int kt = consumed; kt < issued; ++kt)
                 (void)mbar_wait_bounded(&bars[kt % kStages], (uint32_t)(kt / kStages) & 1u);
@@ -266,6 +274,7 @@ cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs
     if (splits < 1) splits = 1;
     const size_t smem = (size_t)kStages * kTile * (sizeof(TriHit) + sizeof(TriBox));
     const bool use_tmp = splits > 1;
+    const int stall_tile = g_tune[SPLAT_TUNE_TEST_WAIT_STALL] - 1;
     if (use_tmp) {
         fill_u64_kernel<<<grid_for(cap, 256, sm_count, 8), 256, 0, s>>>((unsigned long long*)tmp, cap, rays.d_count,
                                                                         (unsigned long long)kNoHit);
@@ -276,11 +285,11 @@ cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs
         if (rays.aos)
             hit_brute_kernel<kRPT, true><<<grid, kBruteThreads, smem, s>>>(
                 rays, recs, boxes, n_recs, per_split, hit_idx, hit_t, use_tmp ? (unsigned long long*)tmp : nullptr,
-                err);
+                err, stall_tile);
         else
             hit_brute_kernel<kRPT, false><<<grid, kBruteThreads, smem, s>>>(
                 rays, recs, boxes, n_recs, per_split, hit_idx, hit_t, use_tmp ? (unsigned long long*)tmp : nullptr,
-                err);
+                err, stall_tile);
         ++g_launches;
     } else {
         // no triangles: every ray misses
@@ -465,7 +474,8 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh_kernel(RaySrc src, BvhVie
                                                               float* __restrict__ hit_t, int32_t* err) {
     const int64_t n = src.d_count ? *src.d_count : src.n;
     int2 stack[kBvhStack];  // (ref, entry distance bits)
-    for_each_ray(n, src.fetch, [&](int64_t k) {
+    for_each_ray(n, src.fetch, [&](int64_t kk) {
+        const int64_t k = src.perm ? (int64_t)src.perm[kk] : kk;
         const HitRay r = load_hit_ray<AOS>(src, k);
         const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
         const float oix = r.ox * ix, oiy = r.oy * iy, oiz = r.oz * iz;
@@ -577,7 +587,8 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_kernel(RaySrc src, Bvh4V
                                                                float* __restrict__ hit_t, int32_t* err) {
     const int64_t n = src.d_count ? *src.d_count : src.n;
     int2 stack[kBvhStack];
-    for_each_ray(n, src.fetch, [&](int64_t k) {
+    for_each_ray(n, src.fetch, [&](int64_t kk) {
+        const int64_t k = src.perm ? (int64_t)src.perm[kk] : kk;
         const HitRay r = load_hit_ray<AOS>(src, k);
         float best;
         int32_t bi;
@@ -595,12 +606,14 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_refill_kernel(RaySrc src
                                                                       float* __restrict__ hit_t, int32_t* err,
                                                                       int refill_min) {
     const int64_t n = src.d_count ? *src.d_count : src.n;
+    auto ray_of = [&](int64_t k) { return src.perm ? (int64_t)src.perm[k] : k; };
     bvh4_refill_loop(
-        n, src.fetch, refill_min, err, [&](int64_t k) { return load_hit_ray<AOS>(src, k); },
+        n, src.fetch, refill_min, err, [&](int64_t k) { return load_hit_ray<AOS>(src, ray_of(k)); },
         [&](int64_t) { return bvh; },
         [&](int64_t k, float best, int32_t bi) {
-            hit_idx[k] = bi;
-            if (hit_t) hit_t[k] = best;
+            const int64_t kk = ray_of(k);
+            hit_idx[kk] = bi;
+            if (hit_t) hit_t[kk] = best;
         });
 }
 
@@ -653,9 +666,10 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_packet_kernel(RaySrc src
     }
     int2 lane_stack[ADAPT ? kBvhStack : 1];
     for_each_warp_batch(n, src.fetch, [&](int64_t base) {
-        const int64_t k = base + lane;
-        const bool valid = k < n;
-        const HitRay r = load_hit_ray<AOS>(src, valid ? k : base);
+        const bool valid = base + lane < n;
+        const int64_t kk = valid ? base + lane : base;
+        const int64_t k = src.perm ? (int64_t)src.perm[kk] : kk;
+        const HitRay r = load_hit_ray<AOS>(src, k);
         float best;
         int32_t bi;
         bool packet = true;
@@ -775,7 +789,7 @@ __device__ __forceinline__ void padded_box(const float* p, float pad_abs, float 
 
 __global__ void pack_hits_kernel(const splat_ftri_t* __restrict__ ftri, int64_t n_tris, TriHit* brute, TriBox* boxes,
                                  const unsigned* __restrict__ scale, const int32_t* __restrict__ bvh_order,
-                                 TriHit* bvh) {
+                                 TriHit* bvh, int32_t* bvh_pos) {
     const float pad_abs = pad_abs_of_scale(__uint_as_float(*scale));
     for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j + 1 < n_tris;
          j += (int64_t)gridDim.x * blockDim.x) {
@@ -789,18 +803,24 @@ __global__ void pack_hits_kernel(const splat_ftri_t* __restrict__ ftri, int64_t 
             const int32_t idx = bvh_order[j];
             const float* q = ftri[idx - 1].v[0];
             bvh[j] = pack_one(idx, f3(q), f3(q + 3), f3(q + 6), f3(q + 9));
+            if (bvh_pos) bvh_pos[idx] = (int32_t)j;
         }
+    }
+    if (bvh_pos && blockIdx.x == 0 && threadIdx.x == 0) {
+        bvh_pos[0] = 0;
+        bvh_pos[1] = 0;  // the sentinel
     }
 }
 
 cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, TriBox* brute_boxes,
-                             unsigned* scale, const int32_t* bvh_order, TriHit* bvh_recs, cudaStream_t s) {
+                             unsigned* scale, const int32_t* bvh_order, TriHit* bvh_recs, int32_t* bvh_pos,
+                             cudaStream_t s) {
     if (n_tris <= 1) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(scale, 0, sizeof(unsigned), s);
     if (e != cudaSuccess) return e;
     scene_scale_kernel<<<grid_for(n_tris, 256, 152, 8), 256, 0, s>>>(ftri, n_tris, scale);
     pack_hits_kernel<<<grid_for(n_tris, 256, 152, 8), 256, 0, s>>>(ftri, n_tris, brute_recs, brute_boxes, scale,
-                                                                    bvh_order, bvh_recs);
+                                                                    bvh_order, bvh_recs, bvh_order ? bvh_pos : nullptr);
     g_launches += 2;
     return cudaGetLastError();
 }

@@ -97,6 +97,28 @@ __device__ __forceinline__ float comp(const float4& v, int i) {
     return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
+// Entry and exit distances of a ray through the four child boxes of a
+// node.  The slab planes are picked by the signs of the inverse direction
+// (ix < 0: the near x plane is hi, else lo), through the addresses of the
+// node's per-axis float4s, so the test needs no per-axis min / max: each
+// distance is the one min(a, b) / max(a, b) of the two planes would pick,
+// bit for bit (lo <= hi for every real child; the empty slots, lo = +inf and
+// hi = -inf, come out with tmin > tmax, and the child count rejects them
+// anyway).
+__device__ __forceinline__ void node4_slabs(const Bvh4Node* nd, float ix, float iy, float iz, float oix, float oiy,
+                                            float oiz, float tmin[4], float tmax[4]) {
+    const float4* q = reinterpret_cast<const float4*>(nd);  // lox, hix, loy, hiy, loz, hiz
+    const int sx = ix < 0.0f ? 1 : 0, sy = iy < 0.0f ? 1 : 0, sz = iz < 0.0f ? 1 : 0;
+    const float4 nx = __ldg(q + sx), fx = __ldg(q + 1 - sx);
+    const float4 ny = __ldg(q + 2 + sy), fy = __ldg(q + 3 - sy);
+    const float4 nz = __ldg(q + 4 + sz), fz = __ldg(q + 5 - sz);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        tmin[i] = fmaxf(fmaxf(fmaf(comp(nx, i), ix, -oix), fmaf(comp(ny, i), iy, -oiy)), fmaf(comp(nz, i), iz, -oiz));
+        tmax[i] = fminf(fminf(fmaf(comp(fx, i), ix, -oix), fmaf(comp(fy, i), iy, -oiy)), fmaf(comp(fz, i), iz, -oiz));
+    }
+}
+
 #define SPLAT_CSWAP(ka, ra, kb, rb)       \
     if (kb < ka) {                         \
         const float tk = ka;               \
@@ -126,21 +148,14 @@ __device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bv
     while (true) {
         if (ref >= 0) {
             const Bvh4Node* nd = bvh.nodes + ref;
-            const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix);
-            const float4 ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
-            const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
             const int4 c = __ldg(&nd->c);
             const int nc = __ldg(&nd->meta.x);
-            float key[4];
+            float tmin[4], tmax[4], key[4];
+            node4_slabs(nd, ix, iy, iz, oix, oiy, oiz, tmin, tmax);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const float a0 = fmaf(comp(lx, i), ix, -oix), b0 = fmaf(comp(hx, i), ix, -oix);
-                const float a1 = fmaf(comp(ly, i), iy, -oiy), b1 = fmaf(comp(hy, i), iy, -oiy);
-                const float a2 = fmaf(comp(lz, i), iz, -oiz), b2 = fmaf(comp(hz, i), iz, -oiz);
-                const float tmin = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fminf(a2, b2));
-                const float tmax = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fmaxf(a2, b2));
-                const bool h = (i < nc) & (tmin <= tmax) & (tmax >= 0.0f) & (tmin <= best);
-                key[i] = h ? fminf(tmin, kMax) : kInf;
+                const bool h = (i < nc) & (tmin[i] <= tmax[i]) & (tmax[i] >= 0.0f) & (tmin[i] <= best);
+                key[i] = h ? fminf(tmin[i], kMax) : kInf;
             }
             float k0 = key[0], k1 = key[1], k2 = key[2], k3 = key[3];
             int r0 = c.x, r1 = c.y, r2 = c.z, r3 = c.w;
@@ -255,21 +270,14 @@ __device__ __forceinline__ void bvh4_refill_loop(int64_t n, unsigned long long* 
             sp = 0;
         } else if (node >= 0) {
             const Bvh4Node* nd = bvh.nodes + node;
-            const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix);
-            const float4 ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
-            const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
             const int4 c = __ldg(&nd->c);
             const int nc = __ldg(&nd->meta.x);
-            float key[4];
+            float tmin[4], tmax[4], key[4];
+            node4_slabs(nd, ix, iy, iz, oix, oiy, oiz, tmin, tmax);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const float a0 = fmaf(comp(lx, i), ix, -oix), b0 = fmaf(comp(hx, i), ix, -oix);
-                const float a1 = fmaf(comp(ly, i), iy, -oiy), b1 = fmaf(comp(hy, i), iy, -oiy);
-                const float a2 = fmaf(comp(lz, i), iz, -oiz), b2 = fmaf(comp(hz, i), iz, -oiz);
-                const float tmin = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fminf(a2, b2));
-                const float tmax = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fmaxf(a2, b2));
-                const bool h = (i < nc) & (tmin <= tmax) & (tmax >= 0.0f) & (tmin <= best);
-                key[i] = h ? fminf(tmin, kMax) : kInf;
+                const bool h = (i < nc) & (tmin[i] <= tmax[i]) & (tmax[i] >= 0.0f) & (tmin[i] <= best);
+                key[i] = h ? fminf(tmin[i], kMax) : kInf;
             }
             float k0 = key[0], k1 = key[1], k2 = key[2], k3 = key[3];
             int r0 = c.x, r1 = c.y, r2 = c.z, r3 = c.w;
@@ -348,21 +356,15 @@ __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid,
     while (true) {
         if (ref >= 0) {
             const Bvh4Node* nd = bvh.nodes + ref;
-            const float4 lx = __ldg(&nd->lox), hx = __ldg(&nd->hix);
-            const float4 ly = __ldg(&nd->loy), hy = __ldg(&nd->hiy);
-            const float4 lz = __ldg(&nd->loz), hz = __ldg(&nd->hiz);
             const int4 c = __ldg(&nd->c);
             const int nc = __ldg(&nd->meta.x);
+            float tmin[4], tmax[4];
+            node4_slabs(nd, ix, iy, iz, oix, oiy, oiz, tmin, tmax);
             unsigned u[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const float a0 = fmaf(comp(lx, i), ix, -oix), b0 = fmaf(comp(hx, i), ix, -oix);
-                const float a1 = fmaf(comp(ly, i), iy, -oiy), b1 = fmaf(comp(hy, i), iy, -oiy);
-                const float a2 = fmaf(comp(lz, i), iz, -oiz), b2 = fmaf(comp(hz, i), iz, -oiz);
-                const float tmin = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fminf(a2, b2));
-                const float tmax = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fmaxf(a2, b2));
-                const bool h = valid & (i < nc) & (tmin <= tmax) & (tmax >= 0.0f) & (tmin <= best);
-                u[i] = __reduce_min_sync(0xffffffffu, h ? monotonic_u32(tmin) : 0xffffffffu);
+                const bool h = valid & (i < nc) & (tmin[i] <= tmax[i]) & (tmax[i] >= 0.0f) & (tmin[i] <= best);
+                u[i] = __reduce_min_sync(0xffffffffu, h ? monotonic_u32(tmin[i]) : 0xffffffffu);
             }
             unsigned k0 = u[0], k1 = u[1], k2 = u[2], k3 = u[3];
             int r0 = c.x, r1 = c.y, r2 = c.z, r3 = c.w;

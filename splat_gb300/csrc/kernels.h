@@ -27,6 +27,8 @@ struct RaySrc {
     int64_t n;                 // ray count when d_count is null
     unsigned long long* fetch; // zeroed work counter: warps take rays 32 at a time (nullptr: grid-stride)
     int32_t packet;            // four-wide BVH: warp packet traversal (1) or one ray per lane (0)
+    const int32_t* perm;       // BVH hitters: the k-th ray traced is ray perm[k] (nullptr: ray k); results
+                               // go to the ray's own index
 };
 
 // Flattened BVH2 node (Aila & Laine 2009 layout): the boxes of both children
@@ -95,10 +97,25 @@ size_t lbvh_scratch_bytes(int64_t n_prims);
 cudaError_t launch_lbvh_build(const splat_ftri_t* ftri, int64_t n_tris, int leaf_max, void* scratch,
                               BvhNode* nodes2, Bvh4Node* nodes4, int32_t* order, int sm_count, cudaStream_t s);
 
+// Coherent ray order (lbvh.cu): a permutation of the d_count active rays of
+// a SoA bounce buffer, grouped by (direction octant, BVH-order position of
+// the triangle the ray leaves) with a counting sort over a key of key_bits
+// (4..20) bits (the position's low bits dropped to fit).  Rays that leave
+// neighbouring triangles in similar directions then share warps, so the
+// traversal's lanes take similar paths.  bvh_pos[i]: BVH record position of
+// reference index i (0 for indices outside 1..n_tris).  *perm_out points
+// into scratch.
+size_t ray_order_bytes(int64_t cap);
+cudaError_t launch_ray_order(const float* soa_f, const int32_t* ignore, int64_t cap, const int64_t* d_count,
+                             const int32_t* bvh_pos, int64_t n_tris, int key_bits, void* scratch,
+                             const int32_t** perm_out, int sm_count, cudaStream_t s);
+
 // scene packing / refit.  scale: device word holding max |vertex coordinate|
 // (float bits), from which every padded box takes pad_abs = 1e-4 max(1, scale).
+// bvh_pos (optional, n_tris + 1 entries): the inverse of bvh_order.
 cudaError_t launch_pack_hits(const splat_ftri_t* ftri, int64_t n_tris, TriHit* brute_recs, TriBox* brute_boxes,
-                             unsigned* scale, const int32_t* bvh_order, TriHit* bvh_recs, cudaStream_t s);
+                             unsigned* scale, const int32_t* bvh_order, TriHit* bvh_recs, int32_t* bvh_pos,
+                             cudaStream_t s);
 
 
 // generation and conversion

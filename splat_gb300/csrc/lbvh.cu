@@ -114,8 +114,9 @@ cudaError_t scan_u32(uint32_t* a, int64_t m, uint32_t* sums, cudaStream_t s) {
 // exclusive scan of the whole array, hist[d * tiles + tile] is where the
 // tile's first key with digit d goes.
 __global__ void radix_hist_kernel(const uint32_t* __restrict__ keys, int64_t n, int shift, uint32_t* hist,
-                                  int64_t tiles) {
+                                  int64_t tiles, const int64_t* d_n) {
     __shared__ uint32_t cnt[256];
+    if (d_n) n = min(n, *d_n);  // key count on the device (at most n)
     cnt[threadIdx.x] = 0;
     __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * kTile;
@@ -133,8 +134,9 @@ __global__ void radix_hist_kernel(const uint32_t* __restrict__ keys, int64_t n, 
 // lanes of its warp (__match_any_sync peers).
 __global__ void radix_scatter_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, int64_t n,
                                      int shift, const uint32_t* __restrict__ hist, int64_t tiles, uint32_t* keys_out,
-                                     uint32_t* vals_out) {
+                                     uint32_t* vals_out, const int64_t* d_n) {
     __shared__ uint32_t s_run[256];
+    if (d_n) n = min(n, *d_n);
     __shared__ uint32_t s_warp[kSortThreads / 32][256];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     s_run[threadIdx.x] = 0;
@@ -511,11 +513,11 @@ cudaError_t launch_lbvh_build(const splat_ftri_t* ftri, int64_t n_tris, int leaf
     g_launches += 3;
     int cur = 0;
     for (int shift = 0; shift < 32; shift += 8) {
-        radix_hist_kernel<<<(unsigned)tiles, kSortThreads, 0, s>>>(keys[cur], n, shift, hist, tiles);
+        radix_hist_kernel<<<(unsigned)tiles, kSortThreads, 0, s>>>(keys[cur], n, shift, hist, tiles, nullptr);
         ++g_launches;
         if ((e = scan_u32(hist, m_hist, sums, s)) != cudaSuccess) return e;
         radix_scatter_kernel<<<(unsigned)tiles, kSortThreads, 0, s>>>(keys[cur], vals[cur], n, shift, hist, tiles,
-                                                                      keys[cur ^ 1], vals[cur ^ 1]);
+                                                                      keys[cur ^ 1], vals[cur ^ 1], nullptr);
         ++g_launches;
         cur ^= 1;
     }
@@ -542,6 +544,96 @@ cudaError_t launch_lbvh_build(const splat_ftri_t* ftri, int64_t n_tris, int leaf
     }
     lbvh_order_kernel<<<grid(n), 256, 0, s>>>(vals[cur], n, order);
     ++g_launches;
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------- ray order
+// A counting sort of the active rays by key: the direction octant above the
+// BVH-order position of the triangle the ray leaves (ignore_tri), the
+// position's low bits dropped so that the key has key_bits bits.  Bucket
+// sizes are counted with global atomics, scanned into offsets, and every ray
+// takes a slot in its bucket with one atomic per group of equal keys in a
+// warp (__match_any_sync), so a warp's rays of one bucket stay together.
+// The order inside a bucket is the atomics' order: only which rays share a
+// warp changes with it, never a result.
+constexpr int kOrderMaxBits = 20;
+
+__device__ __forceinline__ uint32_t ray_key(const float* __restrict__ f, int64_t cap, const int32_t* __restrict__ ignore,
+                                            const int32_t* __restrict__ bvh_pos, int64_t n_tris, int pos_shift,
+                                            int pos_bits, int64_t k) {
+    const uint32_t oct = (f[3 * cap + k] < 0.0f ? 1u : 0u) | (f[4 * cap + k] < 0.0f ? 2u : 0u) |
+                         (f[5 * cap + k] < 0.0f ? 4u : 0u);
+    const int32_t ig = ignore[k];
+    const uint32_t pos = (ig >= 1 && (int64_t)ig <= n_tris) ? (uint32_t)bvh_pos[ig] : 0u;
+    return (oct << pos_bits) | (pos >> pos_shift);
+}
+
+__global__ void ray_bucket_count_kernel(const float* __restrict__ f, int64_t cap, const int32_t* __restrict__ ignore,
+                                        const int64_t* __restrict__ d_count, const int32_t* __restrict__ bvh_pos,
+                                        int64_t n_tris, int pos_shift, int pos_bits, uint32_t* keys, uint32_t* cnt) {
+    const int64_t n = min(cap, *d_count);
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t key = ray_key(f, cap, ignore, bvh_pos, n_tris, pos_shift, pos_bits, k);
+        keys[k] = key;
+        atomicAdd(&cnt[key], 1u);
+    }
+}
+
+__global__ void ray_bucket_place_kernel(const uint32_t* __restrict__ keys, int64_t cap,
+                                        const int64_t* __restrict__ d_count, uint32_t* off, int32_t* perm) {
+    const int64_t n = min(cap, *d_count);
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    // warp-uniform trip count: every lane takes part in the vote
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += stride) {
+        const int64_t k = base + lane;
+        const bool valid = k < n;
+        const uint32_t key = valid ? keys[k] : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t slot = 0;
+        if (valid && lane == leader) slot = atomicAdd(&off[key], (uint32_t)__popc(peers));
+        slot = __shfl_sync(0xffffffffu, slot, leader);
+        if (valid) perm[slot + (uint32_t)__popc(peers & below)] = (int32_t)k;
+    }
+}
+
+size_t ray_order_bytes(int64_t cap) {
+    if (cap < 1) return 256;
+    const int64_t buckets = int64_t(1) << kOrderMaxBits;
+    auto al = [](size_t b) { return (b + 255) / 256 * 256; };
+    return 256 + 2 * al(4 * (size_t)cap) + al(4 * (size_t)buckets) + al(4 * (size_t)n_tiles_of(buckets));
+}
+
+cudaError_t launch_ray_order(const float* soa_f, const int32_t* ignore, int64_t cap, const int64_t* d_count,
+                             const int32_t* bvh_pos, int64_t n_tris, int key_bits, void* scratch,
+                             const int32_t** perm_out, int sm_count, cudaStream_t s) {
+    if (cap < 1) return cudaSuccess;
+    if (key_bits < 4) key_bits = 4;
+    if (key_bits > kOrderMaxBits) key_bits = kOrderMaxBits;
+    const int64_t buckets = int64_t(1) << key_bits;
+    Carve c{reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(scratch) + 255) / 256 * 256)};
+    uint32_t* keys = c.take<uint32_t>(cap);
+    int32_t* perm = c.take<int32_t>(cap);
+    uint32_t* cnt = c.take<uint32_t>(int64_t(1) << kOrderMaxBits);
+    uint32_t* sums = c.take<uint32_t>(n_tiles_of(int64_t(1) << kOrderMaxBits));
+    int full_bits = 1;
+    while (full_bits < 31 && (int64_t(1) << full_bits) < n_tris + 1) ++full_bits;
+    const int pos_bits = full_bits < key_bits - 3 ? full_bits : key_bits - 3;
+    const int pos_shift = full_bits - pos_bits;
+    int64_t b = (cap + 255) / 256;
+    if (b > (int64_t)sm_count * 8) b = (int64_t)sm_count * 8;
+    if (b < 1) b = 1;
+    cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (size_t)buckets, s);
+    if (e != cudaSuccess) return e;
+    ray_bucket_count_kernel<<<(unsigned)b, 256, 0, s>>>(soa_f, cap, ignore, d_count, bvh_pos, n_tris, pos_shift,
+                                                        pos_bits, keys, cnt);
+    ++g_launches;
+    if ((e = scan_u32(cnt, buckets, sums, s)) != cudaSuccess) return e;
+    ray_bucket_place_kernel<<<(unsigned)b, 256, 0, s>>>(keys, cap, d_count, cnt, perm);
+    ++g_launches;
+    *perm_out = perm;
     return cudaGetLastError();
 }
 

@@ -132,6 +132,9 @@ def test_tuning_knobs_validate_and_round_trip_without_gpu():
         assert lib.splat_set_tuning(L.TUNE_TRACE_SPLIT, 0) == L.ERR_INVALID
         assert lib.splat_set_tuning(L.TUNE_TRACE_SPLIT, 5) == L.ERR_INVALID
         assert lib.splat_set_tuning(L.TUNE_TRACE_SPLIT, 2) == L.OK
+        assert lib.splat_get_tuning(L.TUNE_TEST_WAIT_STALL) == 0  # off by default
+        assert lib.splat_set_tuning(L.TUNE_TEST_WAIT_STALL, -1) == L.ERR_INVALID
+        assert lib.splat_set_tuning(L.TUNE_TEST_WAIT_STALL, 0) == L.OK
         assert lib.splat_set_tuning(L.TUNE_KEYS, 1) == L.ERR_INVALID
         assert lib.splat_get_tuning(L.TUNE_KEYS) == -1 and lib.splat_get_tuning(-1) == -1
     finally:

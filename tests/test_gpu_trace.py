@@ -84,7 +84,11 @@ def test_sampled_ranges_match_oracle(torch_cuda, make):
     scene = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
     n = wl.n_rays
     h = int(wl.light["res1"]) // wl.upscale
-    for c in (n // 2 + h // 2 - 600, n // 3 + h // 3):
+    centres = [n // 2 + h // 2 - 600, n // 3 + h // 3]
+    if make is S.menger:
+        # the occlusion-heavy sponge: three more ranges across the grid
+        centres += [n // 4 + (3 * h) // 8, (5 * n) // 8 + (5 * h) // 8, (3 * n) // 4 + h // 4]
+    for c in centres:
         got, st = _gpu(wl, c, c + 1200, scene=scene)
         ref_tex, ref_st, _ = O.trace_forward(wl, c, c + 1200)
         assert st["rays_per_bounce"] == [int(x) for x in ref_st[: wl.depth]]
@@ -110,6 +114,63 @@ def test_realtime_full_size_properties(torch_cuda):
     parts = sum(_gpu(wl, lo, hi, scene=scene)[0].astype(np.int64) for lo, hi in zip(cuts[:-1], cuts[1:]))
     assert np.array_equal(parts, a.astype(np.int64))
     assert sa["diffuse"] > n // 2 and a.sum() > 0
+
+
+def test_menger_full_size_properties(torch_cuda):
+    """2^22 rays / 96,013 triangles, depth 6 (the occlusion-heavy sponge):
+    four-wide BVH == binary BVH == brute force at full size, run-to-run
+    identity, and linearity over disjoint ray ranges (int32)."""
+    from splat_gb300 import tracer
+
+    wl = S.menger()
+    scene = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
+    a, sa = _gpu(wl, scene=scene)
+    b, sb = _gpu(wl, scene=scene)
+    assert np.array_equal(a, b) and sa == sb
+    for other in ("bvh2", "brute"):
+        c, sc = _gpu(wl.with_(hitter=other), scene=scene)
+        assert np.array_equal(a, c) and sa["rays_per_bounce"] == sc["rays_per_bounce"], other
+    n = wl.n_rays
+    cuts = [0, n // 5, n // 2 + 31, n - 4096, n]
+    parts = sum(_gpu(wl, lo, hi, scene=scene)[0].astype(np.int64) for lo, hi in zip(cuts[:-1], cuts[1:]))
+    assert np.array_equal(parts, a.astype(np.int64))
+    assert sa["rays_per_bounce"][5] > n // 2 and a.sum() > 0
+
+
+@pytest.mark.parametrize("make", [S.menger, S.realtime], ids=["menger", "realtime"])
+@pytest.mark.parametrize("bits,packet", [(16, 1), (20, 1), (20, 2), (12, 4), (20, 5)])
+def test_ray_order_keeps_every_map(torch_cuda, make, bits, packet):
+    """Secondary rays traced in sorted order (SPLAT_TUNE_RAY_ORDER: octant,
+    BVH position of the triangle left) and the packet forms over them give
+    the compaction-order step's int32 map and statistics bit for bit, on a
+    2^18-ray range of the full-size workload; one small range also against
+    the oracle."""
+    from splat_gb300 import _lib as L
+    from splat_gb300 import tracer
+
+    lib = L.load()
+    keys = (L.TUNE_RAY_ORDER, L.TUNE_BVH_PACKET)
+    old = [lib.splat_get_tuning(k) for k in keys]
+    wl = make()
+    scene = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
+    n = wl.n_rays
+    lo, hi = n // 2 - (1 << 17), n // 2 + (1 << 17)
+    try:
+        L.check(lib.splat_set_tuning(L.TUNE_RAY_ORDER, 0))
+        L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, 1))
+        ref, sref = _gpu(wl, lo, hi, scene=scene)
+        L.check(lib.splat_set_tuning(L.TUNE_RAY_ORDER, bits))
+        L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, packet))
+        got, sg = _gpu(wl, lo, hi, scene=scene)
+        c = n // 2 + 300
+        small, ss = _gpu(wl, c, c + 1000, scene=scene)
+    finally:
+        for k, v in zip(keys, old):
+            L.check(lib.splat_set_tuning(k, v))
+    assert sg == sref and np.array_equal(got, ref) and ref.sum() > 0
+    ref_tex, ref_st, _ = O.trace_forward(wl, c, c + 1000)
+    assert ss["rays_per_bounce"] == [int(x) for x in ref_st[: wl.depth]]
+    _cmp(wl, small, ref_tex)
 
 
 def test_host_entry_point_matches_device(torch_cuda):
