@@ -511,10 +511,24 @@ enum {
                                             order; 4..20 each bounce after the first groups its rays by (direction
                                             octant, BVH position of the triangle they leave), a key of that many
                                             bits, before the hit launch (default 0) */
-    SPLAT_TUNE_KEYS = 11
+    SPLAT_TUNE_BRUTE_TILE = 11,          /* brute-force hitter: hit records per stage of its shared-memory ring,
+                                            32, 64 (default) or 128 */
+    SPLAT_TUNE_COUNT_WORK = 12,          /* four-wide BVH: 0 (default) plain kernels; 1 counting kernels that add
+                                            their traversal work to counters read by splat_hit_work */
+    SPLAT_TUNE_KEYS = 13
 };
 splat_status_t splat_set_tuning(int32_t key, int32_t value);
 int32_t splat_get_tuning(int32_t key);
+
+/* Traversal work of the four-wide BVH hitter counted while
+ * SPLAT_TUNE_COUNT_WORK is 1, over every device call since the last reset:
+ * out[0] nodes visited, out[1] triangle pre-tests (plane distance and the
+ * conservative "in front of the ray, before the best hit" test), out[2] full
+ * triangle tests (the reference's in_triangle), out[3] rays traced; per ray
+ * lane, so a packet's node visit counts once per valid lane.  No counterpart
+ * in the reference: it feeds the traversal's instruction-issue roofline.
+ * Synchronises the stream; reset != 0 clears the counters after the read. */
+splat_status_t splat_hit_work(int64_t out[4], int32_t reset, void* stream);
 
 /* ------------------------------------------------------------- profiling */
 /* Launch profiling: while a profile is attached to the calling thread, every

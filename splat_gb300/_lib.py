@@ -141,6 +141,7 @@ SIGNATURES = {
     "splat_server_step": ([vp, vp, vp, vp], i32),
     "splat_server_poll": ([vp, i32, vp, vp, i32, vp], i32),
     "splat_server_status": ([vp, vp, vp, vp], i32),
+    "splat_hit_work": ([vp, i32, vp], i32),
     "splat_set_tuning": ([i32, i32], i32),
     "splat_get_tuning": ([i32], i32),
     "splat_profile_create": ([i32, vp], i32),
@@ -161,7 +162,9 @@ TUNE_BVH_REFILL = 7
 TUNE_TRACE_SPLIT = 8
 TUNE_TEST_WAIT_STALL = 9
 TUNE_RAY_ORDER = 10
-TUNE_KEYS = 11
+TUNE_BRUTE_TILE = 11
+TUNE_COUNT_WORK = 12
+TUNE_KEYS = 13
 
 KERNEL_GENERATE = 0
 KERNEL_HIT_BRUTE = 1

@@ -124,7 +124,17 @@ class Lanes:
     ticks then overlap the other lanes' work.  Every frame's map is still
     the one it gets alone."""
 
-    def __init__(self, n_lanes: int, frames: Sequence, scenes: Sequence, maps: Sequence):
+    def __init__(self, n_lanes: int, frames: Sequence, scenes: Sequence, maps: Sequence,
+                 crossover_tris: Optional[int] = None):
+        """crossover_tris (autotune.batch_crossover): frames with fewer
+        triangles are traced by brute force, the others by the four-wide
+        BVH; None keeps each frame's own hitter.  The choices are in
+        `hitters`."""
+        if crossover_tris is not None:
+            from .autotune import hitter_for
+
+            frames = [w.with_(hitter=hitter_for(int(w.n_tris), int(crossover_tris))) for w in frames]
+        self.hitters = [w.hitter for w in frames]
         order = sorted(range(len(frames)), key=lambda i: -frames[i].n_rays)
         load = [0] * n_lanes
         self.members: List[List[int]] = [[] for _ in range(n_lanes)]

@@ -1005,6 +1005,14 @@ splat_status_t splat_trace_forward_host(splat_scene_t* scene, const splat_ftri_t
     return SPLAT_OK;
 }
 
+splat_status_t splat_hit_work(int64_t out[4], int32_t reset, void* stream) {
+    if (!out) return fail(SPLAT_ERR_INVALID, "hit_work: null output");
+    uint64_t w[4] = {0, 0, 0, 0};
+    SPLAT_CUDA(read_hit_work(w, reset != 0, reinterpret_cast<cudaStream_t>(stream)), "hit_work");
+    for (int i = 0; i < 4; ++i) out[i] = (int64_t)w[i];
+    return SPLAT_OK;
+}
+
 splat_status_t splat_set_tuning(int32_t key, int32_t value) {
     if (key < 0 || key >= SPLAT_TUNE_KEYS) return fail(SPLAT_ERR_INVALID, "set_tuning: unknown key");
     if (key == SPLAT_TUNE_SPLAT_AGGREGATE) {
@@ -1017,6 +1025,11 @@ splat_status_t splat_set_tuning(int32_t key, int32_t value) {
         if (value < 0 || value > 32) return fail(SPLAT_ERR_INVALID, "set_tuning: refill threshold must be 0..32");
     } else if (key == SPLAT_TUNE_TRACE_SPLIT) {
         if (value < 1 || value > kMaxTraceParts) return fail(SPLAT_ERR_INVALID, "set_tuning: split must be 1..4");
+    } else if (key == SPLAT_TUNE_COUNT_WORK) {
+        if (value != 0 && value != 1) return fail(SPLAT_ERR_INVALID, "set_tuning: count work must be 0 or 1");
+    } else if (key == SPLAT_TUNE_BRUTE_TILE) {
+        if (value != 32 && value != 64 && value != 128)
+            return fail(SPLAT_ERR_INVALID, "set_tuning: brute tile must be 32, 64 or 128");
     } else if (key == SPLAT_TUNE_RAY_ORDER) {
         if (value != 0 && (value < 4 || value > 20))
             return fail(SPLAT_ERR_INVALID, "set_tuning: ray order bits must be 0 or 4..20");
@@ -1132,6 +1145,8 @@ struct splat_batch {
     bool overlap = false;    // set while capturing with the overlap
     int32_t cap_t1 = 0;      // host tick after the captured ticks
     int cap_parity1 = 0;     // buffer parity after them
+    int32_t cap_t0 = 0;      // host tick and parity the captured ticks start from
+    int cap_parity0 = 0;
 };
 
 namespace {
@@ -1439,6 +1454,18 @@ splat_status_t splat_batch_status(const splat_batch_t* b, int32_t* in_flight, in
 splat_status_t splat_batch_capture(splat_batch_t* b, void* stream, int32_t* n_ticks) {
     if (!b) return fail(SPLAT_ERR_INVALID, "batch_capture: null batch");
     cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    // capturing again the item set a replay has just run (nothing admitted
+    // since): start from the previous capture's first tick again, so the
+    // same frames are captured with the launch shapes now set
+    if (b->exec && b->tick == b->cap_t1) {
+        bool fresh = false;
+        for (int32_t s = 0; s < b->max_items; ++s)
+            if (b->used[(size_t)s] && b->start[(size_t)s] >= b->cap_t1) fresh = true;
+        if (!fresh) {
+            b->tick = b->cap_t0;
+            b->parity = b->cap_parity0;
+        }
+    }
     int32_t last = b->tick - 1;
     for (int32_t s = 0; s < b->max_items; ++s) {
         if (!b->used[(size_t)s] || b->start[(size_t)s] + b->depth[(size_t)s] - 1 < b->tick) continue;
@@ -1482,6 +1509,8 @@ splat_status_t splat_batch_capture(splat_batch_t* b, void* stream, int32_t* n_ti
     // the captured ticks have not run yet: each replay runs them
     b->cap_t1 = b->tick;
     b->cap_parity1 = b->parity;
+    b->cap_t0 = t0;
+    b->cap_parity0 = p0;
     b->tick = t0;
     b->parity = p0;
     return SPLAT_OK;

@@ -310,7 +310,7 @@ cudaError_t launch_batch_trace(const BatchTickArgs& a, cudaStream_t s) {
                                                     a.sm_count, 128, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]),
                                       128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch);
         ++g_launches;
-        const int eg = grid_cap(a.cap_rays, kBatchThreads, a.sm_count, 8);
+        const int eg = grid_cap(a.cap_rays, kBatchThreads, a.sm_count, g_tune[SPLAT_TUNE_EVOLVE_BLOCKS_PER_SM]);
 #define SPLAT_BATCH_EVOLVE(MK)                                                                            \
     batch_evolve_kernel<MK><<<eg, kBatchThreads, 0, s>>>(a.cur, a.next, a.queue, a.cur_count, a.next_count, \
                                                          a.queue_count, items, a.tick, a.hit_idx, a.err)
@@ -329,10 +329,11 @@ cudaError_t launch_batch_trace(const BatchTickArgs& a, cudaStream_t s) {
 cudaError_t launch_batch_splat(const BatchTickArgs& a, cudaStream_t s) {
     if (a.cap_rays <= 0) return cudaSuccess;
     const BatchItem* items = reinterpret_cast<const BatchItem*>(a.items);
+    const int sg = grid_cap(a.cap_rays, 256, a.sm_count, g_tune[SPLAT_TUNE_SPLAT_BLOCKS_PER_SM]);
     if (g_tune[SPLAT_TUNE_SPLAT_AGGREGATE])
-        batch_splat_agg_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count, items);
+        batch_splat_agg_kernel<<<sg, 256, 0, s>>>(a.queue, a.queue_count, items);
     else
-        batch_splat_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(a.queue, a.queue_count, items);
+        batch_splat_kernel<<<sg, 256, 0, s>>>(a.queue, a.queue_count, items);
     ++g_launches;
     return cudaGetLastError();
 }

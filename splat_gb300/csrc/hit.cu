@@ -24,7 +24,7 @@
 namespace splat {
 
 thread_local int64_t g_launches = 0;
-std::atomic<int32_t> g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1, 2, 0, 2, 0, 0};
+std::atomic<int32_t> g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1, 2, 0, 2, 0, 0, 64, 0};
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + bulk copy (sm_90+ async proxy)
@@ -73,10 +73,12 @@ constexpr uint32_t kStallPolls = 64;
 // brute force, TMA-staged tiles
 // ---------------------------------------------------------------------------
 constexpr int kBruteThreads = 256;
-constexpr int kTile = 64;
+constexpr int kTile = 64;  // records per tile of the n_tris drop-in kernel
 constexpr int kStages = 4;
 
-template <int RPT, bool AOS>
+// TILE: hit records per stage of the ring (SPLAT_TUNE_BRUTE_TILE: 32, 64 or
+// 128); the ring holds kStages x TILE x 112 bytes of shared memory.
+template <int RPT, bool AOS, int TILE>
 __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, const TriHit* __restrict__ recs,
                                                                   const TriBox* __restrict__ boxes,
                                                                   int64_t n_recs, int64_t per_split,
@@ -86,7 +88,7 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
                                                                   int32_t* err, int stall_tile) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TriHit* tiles = reinterpret_cast<TriHit*>(smem_raw);
-    TriBox* btiles = reinterpret_cast<TriBox*>(smem_raw + (size_t)kStages * kTile * sizeof(TriHit));
+    TriBox* btiles = reinterpret_cast<TriBox*>(smem_raw + (size_t)kStages * TILE * sizeof(TriHit));
     __shared__ __align__(8) uint64_t bars[kStages];
     // stall_tile >= 0 (test only): the wait for that tile polls `stall`, a
     // barrier that no copy and no thread ever completes, kStallPolls times,
@@ -99,7 +101,7 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
     const int64_t tb = (int64_t)blockIdx.y * per_split;
     const int64_t te = min(n_recs, tb + per_split);
     if (tb >= te) return;
-    const int n_tiles = (int)((te - tb + kTile - 1) / kTile);
+    const int n_tiles = (int)((te - tb + TILE - 1) / TILE);
 
     HitRay ray[RPT];
     float best[RPT];
@@ -132,12 +134,12 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
 
     auto issue = [&](int kt) {
         const int s = kt % kStages;
-        const int64_t first = tb + (int64_t)kt * kTile;
-        const uint32_t cnt = (uint32_t)min((int64_t)kTile, te - first);
+        const int64_t first = tb + (int64_t)kt * TILE;
+        const uint32_t cnt = (uint32_t)min((int64_t)TILE, te - first);
         const uint32_t bytes = cnt * (uint32_t)sizeof(TriHit), bbytes = cnt * (uint32_t)sizeof(TriBox);
         mbar_arrive_expect_tx(&bars[s], bytes + bbytes);
-        bulk_g2s(tiles + s * kTile, recs + first, bytes, &bars[s]);
-        bulk_g2s(btiles + s * kTile, boxes + first, bbytes, &bars[s]);
+        bulk_g2s(tiles + s * TILE, recs + first, bytes, &bars[s]);
+        bulk_g2s(btiles + s * TILE, boxes + first, bbytes, &bars[s]);
     };
     if (threadIdx.x == 0) {
         for (int kt = 0; kt < min(kStages, n_tiles); ++kt) issue(kt);
@@ -153,9 +155,9 @@ __global__ void __launch_bounds__(kBruteThreads) hit_brute_kernel(RaySrc src, co
             failed = true;
             break;
         }
-        const int cnt = (int)min((int64_t)kTile, te - (tb + (int64_t)kt * kTile));
-        const TriHit* tile = tiles + s * kTile;
-        const TriBox* btile = btiles + s * kTile;
+        const int cnt = (int)min((int64_t)TILE, te - (tb + (int64_t)kt * TILE));
+        const TriHit* tile = tiles + s * TILE;
+        const TriBox* btile = btiles + s * TILE;
 #pragma unroll 2
         for (int j = 0; j < cnt; ++j) {
             const float4 lo = btile[j].lo, hi = btile[j].hi;
@@ -255,24 +257,44 @@ cudaError_t launch_unpack_hits(const uint64_t* tmp, int64_t n, const int64_t* d_
 
 constexpr int kRPT = 2;
 
+template <int TILE>
+static void launch_brute_tiles(dim3 grid, cudaStream_t s, const RaySrc& rays, const TriHit* recs, const TriBox* boxes,
+                               int64_t n_recs, int64_t per_split, int32_t* hit_idx, float* hit_t,
+                               unsigned long long* tmp, int32_t* err, int stall_tile) {
+    const size_t smem = (size_t)kStages * TILE * (sizeof(TriHit) + sizeof(TriBox));
+    static bool configured = false;  // rings above 48 KB need the opt-in
+    if (!configured) {
+        cudaFuncSetAttribute(hit_brute_kernel<kRPT, true, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(hit_brute_kernel<kRPT, false, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+        configured = true;
+    }
+    if (rays.aos)
+        hit_brute_kernel<kRPT, true, TILE><<<grid, kBruteThreads, smem, s>>>(rays, recs, boxes, n_recs, per_split,
+                                                                             hit_idx, hit_t, tmp, err, stall_tile);
+    else
+        hit_brute_kernel<kRPT, false, TILE><<<grid, kBruteThreads, smem, s>>>(rays, recs, boxes, n_recs, per_split,
+                                                                              hit_idx, hit_t, tmp, err, stall_tile);
+}
+
 cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs, const TriBox* boxes, int64_t n_recs,
                              int32_t* hit_idx, float* hit_t, uint64_t* tmp, int32_t* err, int sm_count,
                              cudaStream_t s) {
     if (cap <= 0) return cudaSuccess;
+    const int tile = g_tune[SPLAT_TUNE_BRUTE_TILE].load();
     const int64_t rays_per_block = (int64_t)kBruteThreads * kRPT;
     const int64_t ray_blocks = (cap + rays_per_block - 1) / rays_per_block;
     // split the triangle range so the grid covers the GPU a few times over
     int64_t splits = ((int64_t)sm_count * g_tune[SPLAT_TUNE_BRUTE_BLOCKS_PER_SM] + ray_blocks - 1) / ray_blocks;
-    const int64_t max_splits = (n_recs + 4 * kTile - 1) / (4 * kTile);
+    const int64_t max_splits = (n_recs + 4 * tile - 1) / (4 * tile);
     if (splits > max_splits) splits = max_splits;
     if (splits < 1) splits = 1;
     if (splits > 65535) splits = 65535;
     if (tmp == nullptr) splits = 1;
     int64_t per_split = (n_recs + splits - 1) / splits;
-    per_split = ((per_split + kTile - 1) / kTile) * kTile;
+    per_split = ((per_split + tile - 1) / tile) * tile;
     splits = (n_recs + per_split - 1) / per_split;
     if (splits < 1) splits = 1;
-    const size_t smem = (size_t)kStages * kTile * (sizeof(TriHit) + sizeof(TriBox));
     const bool use_tmp = splits > 1;
     const int stall_tile = g_tune[SPLAT_TUNE_TEST_WAIT_STALL] - 1;
     if (use_tmp) {
@@ -282,14 +304,13 @@ cudaError_t launch_hit_brute(const RaySrc& rays, int64_t cap, const TriHit* recs
     }
     dim3 grid((unsigned)ray_blocks, (unsigned)splits);
     if (n_recs > 0) {
-        if (rays.aos)
-            hit_brute_kernel<kRPT, true><<<grid, kBruteThreads, smem, s>>>(
-                rays, recs, boxes, n_recs, per_split, hit_idx, hit_t, use_tmp ? (unsigned long long*)tmp : nullptr,
-                err, stall_tile);
+        unsigned long long* t = use_tmp ? (unsigned long long*)tmp : nullptr;
+        if (tile == 32)
+            launch_brute_tiles<32>(grid, s, rays, recs, boxes, n_recs, per_split, hit_idx, hit_t, t, err, stall_tile);
+        else if (tile == 128)
+            launch_brute_tiles<128>(grid, s, rays, recs, boxes, n_recs, per_split, hit_idx, hit_t, t, err, stall_tile);
         else
-            hit_brute_kernel<kRPT, false><<<grid, kBruteThreads, smem, s>>>(
-                rays, recs, boxes, n_recs, per_split, hit_idx, hit_t, use_tmp ? (unsigned long long*)tmp : nullptr,
-                err, stall_tile);
+            launch_brute_tiles<64>(grid, s, rays, recs, boxes, n_recs, per_split, hit_idx, hit_t, t, err, stall_tile);
         ++g_launches;
     } else {
         // no triangles: every ray misses
@@ -581,21 +602,40 @@ cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, 
 // hit children are sorted by entry distance, the nearest is visited next and
 // the others are pushed farthest first together with their entry distance,
 // so a popped entry that lies beyond the current best hit is skipped.
-template <bool AOS>
+// Traversal work of the counting kernels (SPLAT_TUNE_COUNT_WORK): nodes
+// visited, triangle pre-tests, full triangle tests, rays traced.  Every GPU
+// that loads the library holds these four words; splat_hit_work reads and
+// clears them.
+__device__ unsigned long long g_hit_work[4];
+
+__device__ __forceinline__ void flush_work(const WorkCount& wc, uint32_t rays) {
+    unsigned long long v[4] = {wc.nodes, wc.pre, wc.full, rays};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        for (int o = 16; o; o >>= 1) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+        if ((threadIdx.x & 31) == 0 && v[i]) atomicAdd(&g_hit_work[i], v[i]);
+    }
+}
+
+template <bool AOS, bool COUNT>
 __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_kernel(RaySrc src, Bvh4View bvh,
                                                                int32_t* __restrict__ hit_idx,
                                                                float* __restrict__ hit_t, int32_t* err) {
     const int64_t n = src.d_count ? *src.d_count : src.n;
     int2 stack[kBvhStack];
+    WorkCount wc{0u, 0u, 0u};
+    uint32_t rays = 0;
     for_each_ray(n, src.fetch, [&](int64_t kk) {
         const int64_t k = src.perm ? (int64_t)src.perm[kk] : kk;
         const HitRay r = load_hit_ray<AOS>(src, k);
         float best;
         int32_t bi;
-        bvh4_closest(r, bvh, stack, err, best, bi);
+        bvh4_closest(r, bvh, stack, err, best, bi, COUNT ? &wc : nullptr);
+        if (COUNT) ++rays;
         hit_idx[k] = bi;
         if (hit_t) hit_t[k] = best;
     });
+    if (COUNT) flush_work(wc, rays);
 }
 
 
@@ -638,11 +678,13 @@ __device__ __forceinline__ float warp_spread(float a, float b, float c) {
 // on a shared-memory stack.  ADAPT: per warp, packets only when its rays are
 // nearly parallel (direction spread <= dir_spread) and close together (origin
 // spread <= org_spread x the scene's extent); otherwise one ray per lane.
-template <bool AOS, bool ADAPT>
+template <bool AOS, bool ADAPT, bool COUNT = false>
 __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_packet_kernel(RaySrc src, Bvh4View bvh,
                                                                       int32_t* __restrict__ hit_idx,
                                                                       float* __restrict__ hit_t, int32_t* err,
                                                                       float dir_spread, float org_spread) {
+    WorkCount wc{0u, 0u, 0u};
+    uint32_t rays = 0;
     __shared__ int s_stack[kBvhThreads / 32][kPacketStack];
     int* stack = s_stack[threadIdx.x >> 5];
     const int64_t n = src.d_count ? *src.d_count : src.n;
@@ -678,15 +720,17 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_packet_kernel(RaySrc src
             packet = ds <= dir_spread && os <= org_spread * extent;
         }
         if (packet) {
-            bvh4_closest_packet(r, valid, bvh, stack, err, best, bi);
+            bvh4_closest_packet(r, valid, bvh, stack, err, best, bi, COUNT ? &wc : nullptr);
         } else if (ADAPT && valid) {
-            bvh4_closest(r, bvh, lane_stack, err, best, bi);
+            bvh4_closest(r, bvh, lane_stack, err, best, bi, COUNT ? &wc : nullptr);
         }
         if (valid) {
+            if (COUNT) ++rays;
             hit_idx[k] = bi;
             if (hit_t) hit_t[k] = best;
         }
     });
+    if (COUNT) flush_work(wc, rays);
 }
 
 // The traversal kernels use no shared memory: give the whole L1/shared
@@ -696,63 +740,87 @@ static void prefer_l1(K kernel) {
     cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
 }
 
+template <bool COUNT>
+static void launch_bvh4_form(const RaySrc& rays, int64_t cap, const Bvh4View& bvh, int32_t* hit_idx, float* hit_t,
+                             int32_t* err, int sm_count, cudaStream_t s) {
+    const int knob = g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM];
+    auto grid_of = [&](const void* k) {
+        return rays.fetch ? resident_grid(k, cap, sm_count, kBvhThreads, knob) : grid_for(cap, kBvhThreads, sm_count, knob);
+    };
+    if (rays.packet) {
+        // packet = 1: every warp; 2, 3: per warp by ray spread (loose, tight)
+        const float ds = rays.packet == 2 ? 0.3f : 0.1f, os = rays.packet == 2 ? 0.05f : 0.01f;
+        if (rays.packet == 1) {
+            const int grid = grid_of(reinterpret_cast<const void*>(hit_bvh4_packet_kernel<false, false, COUNT>));
+            if (rays.aos)
+                hit_bvh4_packet_kernel<true, false, COUNT><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err,
+                                                                                       ds, os);
+            else
+                hit_bvh4_packet_kernel<false, false, COUNT><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t,
+                                                                                        err, ds, os);
+        } else {
+            const int grid = grid_of(reinterpret_cast<const void*>(hit_bvh4_packet_kernel<false, true, COUNT>));
+            if (rays.aos)
+                hit_bvh4_packet_kernel<true, true, COUNT><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err,
+                                                                                      ds, os);
+            else
+                hit_bvh4_packet_kernel<false, true, COUNT><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err,
+                                                                                       ds, os);
+        }
+        return;
+    }
+    if (!COUNT && rays.fetch && g_tune[SPLAT_TUNE_BVH_REFILL] > 0) {
+        const int grid = resident_grid(reinterpret_cast<const void*>(hit_bvh4_refill_kernel<false>), cap, sm_count,
+                                       kBvhThreads, knob);
+        const int m = g_tune[SPLAT_TUNE_BVH_REFILL];
+        if (rays.aos)
+            hit_bvh4_refill_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, m);
+        else
+            hit_bvh4_refill_kernel<false><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, m);
+        return;
+    }
+    const int grid = grid_of(reinterpret_cast<const void*>(hit_bvh4_kernel<false, COUNT>));
+    if (rays.aos)
+        hit_bvh4_kernel<true, COUNT><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
+    else
+        hit_bvh4_kernel<false, COUNT><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
+}
+
 cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh, int32_t* hit_idx, float* hit_t,
                             int32_t* err, int sm_count, cudaStream_t s) {
     if (cap <= 0) return cudaSuccess;
     static bool configured = false;
     if (!configured) {
-        prefer_l1(hit_bvh4_kernel<true>);
-        prefer_l1(hit_bvh4_kernel<false>);
+        prefer_l1(hit_bvh4_kernel<true, false>);
+        prefer_l1(hit_bvh4_kernel<false, false>);
+        prefer_l1(hit_bvh4_kernel<true, true>);
+        prefer_l1(hit_bvh4_kernel<false, true>);
         prefer_l1(hit_bvh4_refill_kernel<true>);
         prefer_l1(hit_bvh4_refill_kernel<false>);
         prefer_l1(hit_bvh_kernel<true>);
         prefer_l1(hit_bvh_kernel<false>);
         configured = true;
     }
-    if (rays.packet) {
-        // packet = 1: every warp; 2, 3: per warp by ray spread (loose, tight)
-        const float ds = rays.packet == 2 ? 0.3f : 0.1f, os = rays.packet == 2 ? 0.05f : 0.01f;
-        const int knob = g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM];
-        if (rays.packet == 1) {
-            const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh4_packet_kernel<false, false>),
-                                                        cap, sm_count, kBvhThreads, knob)
-                                        : grid_for(cap, kBvhThreads, sm_count, knob);
-            if (rays.aos)
-                hit_bvh4_packet_kernel<true, false><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, ds, os);
-            else
-                hit_bvh4_packet_kernel<false, false><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, ds, os);
-        } else {
-            const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh4_packet_kernel<false, true>),
-                                                        cap, sm_count, kBvhThreads, knob)
-                                        : grid_for(cap, kBvhThreads, sm_count, knob);
-            if (rays.aos)
-                hit_bvh4_packet_kernel<true, true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, ds, os);
-            else
-                hit_bvh4_packet_kernel<false, true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, ds, os);
-        }
-        ++g_launches;
-        return cudaGetLastError();
-    }
-    if (rays.fetch && g_tune[SPLAT_TUNE_BVH_REFILL] > 0) {
-        const int grid = resident_grid(reinterpret_cast<const void*>(hit_bvh4_refill_kernel<false>), cap, sm_count,
-                                       kBvhThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
-        const int m = g_tune[SPLAT_TUNE_BVH_REFILL];
-        if (rays.aos)
-            hit_bvh4_refill_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, m);
-        else
-            hit_bvh4_refill_kernel<false><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err, m);
-        ++g_launches;
-        return cudaGetLastError();
-    }
-    const int grid = rays.fetch ? resident_grid(reinterpret_cast<const void*>(hit_bvh4_kernel<false>), cap, sm_count,
-                                                kBvhThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM])
-                                : grid_for(cap, kBvhThreads, sm_count, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
-    if (rays.aos)
-        hit_bvh4_kernel<true><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
+    if (g_tune[SPLAT_TUNE_COUNT_WORK])
+        launch_bvh4_form<true>(rays, cap, bvh, hit_idx, hit_t, err, sm_count, s);
     else
-        hit_bvh4_kernel<false><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err);
+        launch_bvh4_form<false>(rays, cap, bvh, hit_idx, hit_t, err, sm_count, s);
     ++g_launches;
     return cudaGetLastError();
+}
+
+cudaError_t read_hit_work(uint64_t out[4], bool reset, cudaStream_t s) {
+    cudaError_t e = cudaMemcpyFromSymbolAsync(out, g_hit_work, 4 * sizeof(unsigned long long), 0,
+                                              cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    if (reset) {
+        static const unsigned long long zero[4] = {0ull, 0ull, 0ull, 0ull};
+        if ((e = cudaMemcpyToSymbolAsync(g_hit_work, zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return e;
+        e = cudaStreamSynchronize(s);
+    }
+    return e;
 }
 
 // ---------------------------------------------------------------------------

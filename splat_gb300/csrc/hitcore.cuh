@@ -42,6 +42,14 @@ __device__ __forceinline__ HitRay load_hit_ray(const RaySrc& s, int64_t k) {
     return r;
 }
 
+// Traversal work of one thread, counted only by the counting instantiations
+// of the four-wide kernels (SPLAT_TUNE_COUNT_WORK): nodes visited, triangle
+// pre-tests, full triangle tests.  Kernels that do not count pass nullptr,
+// which removes the counting code.
+struct WorkCount {
+    uint32_t nodes, pre, full;
+};
+
 // Plane terms of distance_to_plane (src/geo.jl:433-435) and a conservative
 // pre-test: an accepted hit has t = num / den > 0 (so num, den are non-zero
 // with one sign) and t <= best; |num| > |den| best (1 + 2^-20), evaluated in
@@ -136,7 +144,7 @@ __device__ __forceinline__ void node4_slabs(const Bvh4Node* nd, float ix, float 
 // skipped.  stack holds kBvhStack entries of (ref, entry distance bits), so
 // a push or a pop is one 8-byte local access.
 __device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bvh, int2* stack, int32_t* err,
-                                             float& best_out, int32_t& bi_out) {
+                                             float& best_out, int32_t& bi_out, WorkCount* wc = nullptr) {
     const float kInf = __int_as_float(0x7f800000);
     const float kMax = 3.402823466e38f;
     const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
@@ -148,6 +156,7 @@ __device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bv
     while (true) {
         if (ref >= 0) {
             const Bvh4Node* nd = bvh.nodes + ref;
+            if (wc) ++wc->nodes;
             const int4 c = __ldg(&nd->c);
             const int nc = __ldg(&nd->meta.x);
             float tmin[4], tmax[4], key[4];
@@ -182,7 +191,9 @@ __device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bv
             for (int j = 0; j < count; ++j) {
                 const TriHit* h = bvh.tris + first + j;
                 float num, den;
+                if (wc) ++wc->pre;
                 if (!tri_candidate(__ldg(&h->n_nv), r, best, num, den)) continue;
+                if (wc) ++wc->full;
                 const float4 q1 = __ldg(&h->a_idx);
                 const int32_t idx = __float_as_int(q1.w);
                 bool inside;
@@ -345,7 +356,8 @@ __device__ __forceinline__ void bvh4_refill_loop(int64_t n, unsigned long long* 
 constexpr int kPacketStack = 128;
 
 __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid, const Bvh4View& bvh, int* stack,
-                                                    int32_t* err, float& best_out, int32_t& bi_out) {
+                                                    int32_t* err, float& best_out, int32_t& bi_out,
+                                                    WorkCount* wc = nullptr) {
     const float kInf = __int_as_float(0x7f800000);
     const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
     const float oix = r.ox * ix, oiy = r.oy * iy, oiz = r.oz * iz;
@@ -356,6 +368,7 @@ __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid,
     while (true) {
         if (ref >= 0) {
             const Bvh4Node* nd = bvh.nodes + ref;
+            if (wc && valid) ++wc->nodes;
             const int4 c = __ldg(&nd->c);
             const int nc = __ldg(&nd->meta.x);
             float tmin[4], tmax[4];
@@ -363,8 +376,14 @@ __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid,
             unsigned u[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const bool h = valid & (i < nc) & (tmin[i] <= tmax[i]) & (tmax[i] >= 0.0f) & (tmin[i] <= best);
-                u[i] = __reduce_min_sync(0xffffffffu, h ? monotonic_u32(tmin[i]) : 0xffffffffu);
+                // t0 = max(tmin, 0): (tmin <= tmax and tmax >= 0) is t0 <= tmax, and
+                // tmin <= best is t0 <= best (best > 0: accepted hits have t > 0).
+                // Non-negative floats order as their bits, so t0's bits are the
+                // sort key (a -0 from the max sorts last: order only, never which
+                // children are entered)
+                const float t0 = fmaxf(tmin[i], 0.0f);
+                const bool h = valid & (i < nc) & (t0 <= tmax[i]) & (t0 <= best);
+                u[i] = __reduce_min_sync(0xffffffffu, h ? __float_as_uint(t0) : 0xffffffffu);
             }
             unsigned k0 = u[0], k1 = u[1], k2 = u[2], k3 = u[3];
             int r0 = c.x, r1 = c.y, r2 = c.z, r3 = c.w;
@@ -401,8 +420,10 @@ __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid,
             for (int j = 0; j < count; ++j) {
                 const TriHit* h = bvh.tris + first + j;
                 float num, den;
+                if (wc && valid) ++wc->pre;
                 const bool cand = valid && tri_candidate(__ldg(&h->n_nv), r, best, num, den);
                 if (!cand) continue;
+                if (wc) ++wc->full;
                 const float4 q1 = __ldg(&h->a_idx);
                 const int32_t idx = __float_as_int(q1.w);
                 bool inside;

@@ -81,6 +81,9 @@ cudaError_t launch_hit_bvh(const RaySrc& rays, int64_t cap, const BvhView& bvh, 
                            int32_t* err, int sm_count, cudaStream_t s);
 cudaError_t launch_hit_bvh4(const RaySrc& rays, int64_t cap, const Bvh4View& bvh, int32_t* hit_idx, float* hit_t,
                             int32_t* err, int sm_count, cudaStream_t s);
+// traversal work counted while SPLAT_TUNE_COUNT_WORK is set (nodes, triangle
+// pre-tests, full triangle tests, rays); synchronises s; reset clears them
+cudaError_t read_hit_work(uint64_t out[4], bool reset, cudaStream_t s);
 // grid of a work-counter traversal launch (one resident wave)
 int resident_grid(const void* kernel, int64_t cap, int sm_count, int threads, int max_per_sm);
 // one-launch bottom-up refit of a two-child (wide = false) or four-wide tree;

@@ -560,22 +560,29 @@ constexpr int kOrderMaxBits = 20;
 
 __device__ __forceinline__ uint32_t ray_key(const float* __restrict__ f, int64_t cap, const int32_t* __restrict__ ignore,
                                             const int32_t* __restrict__ bvh_pos, int64_t n_tris, int pos_shift,
-                                            int pos_bits, int64_t k) {
+                                            uint32_t n_pos, int64_t k) {
     const uint32_t oct = (f[3 * cap + k] < 0.0f ? 1u : 0u) | (f[4 * cap + k] < 0.0f ? 2u : 0u) |
                          (f[5 * cap + k] < 0.0f ? 4u : 0u);
     const int32_t ig = ignore[k];
     const uint32_t pos = (ig >= 1 && (int64_t)ig <= n_tris) ? (uint32_t)bvh_pos[ig] : 0u;
-    return (oct << pos_bits) | (pos >> pos_shift);
+    return oct * n_pos + (pos >> pos_shift);
 }
 
+// Bucket sizes: one atomic per group of equal keys in a warp.
 __global__ void ray_bucket_count_kernel(const float* __restrict__ f, int64_t cap, const int32_t* __restrict__ ignore,
                                         const int64_t* __restrict__ d_count, const int32_t* __restrict__ bvh_pos,
-                                        int64_t n_tris, int pos_shift, int pos_bits, uint32_t* keys, uint32_t* cnt) {
+                                        int64_t n_tris, int pos_shift, uint32_t n_pos, uint32_t* keys,
+                                        uint32_t* cnt) {
     const int64_t n = min(cap, *d_count);
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        const uint32_t key = ray_key(f, cap, ignore, bvh_pos, n_tris, pos_shift, pos_bits, k);
-        keys[k] = key;
-        atomicAdd(&cnt[key], 1u);
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += stride) {
+        const int64_t k = base + lane;
+        const bool valid = k < n;
+        const uint32_t key = valid ? ray_key(f, cap, ignore, bvh_pos, n_tris, pos_shift, n_pos, k) : 0xffffffffu;
+        if (valid) keys[k] = key;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        if (valid && lane == __ffs(peers) - 1) atomicAdd(&cnt[key], (uint32_t)__popc(peers));
     }
 }
 
@@ -612,23 +619,25 @@ cudaError_t launch_ray_order(const float* soa_f, const int32_t* ignore, int64_t 
     if (cap < 1) return cudaSuccess;
     if (key_bits < 4) key_bits = 4;
     if (key_bits > kOrderMaxBits) key_bits = kOrderMaxBits;
-    const int64_t buckets = int64_t(1) << key_bits;
     Carve c{reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(scratch) + 255) / 256 * 256)};
     uint32_t* keys = c.take<uint32_t>(cap);
     int32_t* perm = c.take<int32_t>(cap);
     uint32_t* cnt = c.take<uint32_t>(int64_t(1) << kOrderMaxBits);
     uint32_t* sums = c.take<uint32_t>(n_tiles_of(int64_t(1) << kOrderMaxBits));
+    // positions 0 .. n_tris - 2 (the records); keep the high bits that fit
     int full_bits = 1;
     while (full_bits < 31 && (int64_t(1) << full_bits) < n_tris + 1) ++full_bits;
     const int pos_bits = full_bits < key_bits - 3 ? full_bits : key_bits - 3;
     const int pos_shift = full_bits - pos_bits;
+    const uint32_t n_pos = (uint32_t)((n_tris >> pos_shift) + 1);  // positions after the shift, all < n_pos
+    const int64_t buckets = 8 * (int64_t)n_pos;                     // <= 2^key_bits
     int64_t b = (cap + 255) / 256;
     if (b > (int64_t)sm_count * 8) b = (int64_t)sm_count * 8;
     if (b < 1) b = 1;
     cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (size_t)buckets, s);
     if (e != cudaSuccess) return e;
     ray_bucket_count_kernel<<<(unsigned)b, 256, 0, s>>>(soa_f, cap, ignore, d_count, bvh_pos, n_tris, pos_shift,
-                                                        pos_bits, keys, cnt);
+                                                        n_pos, keys, cnt);
     ++g_launches;
     if ((e = scan_u32(cnt, buckets, sums, s)) != cudaSuccess) return e;
     ray_bucket_place_kernel<<<(unsigned)b, 256, 0, s>>>(keys, cap, d_count, cnt, perm);

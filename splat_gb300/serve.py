@@ -123,7 +123,7 @@ class Server:
 
     def __init__(self, scenes: ScenePool, budget_bytes: int, max_items: int = 128, max_pool_rays: int = 1 << 24,
                  max_ticks_ahead: int = 4, lanes: int = 2, split_min_rays: Optional[int] = None,
-                 on_done: Optional[Callable[[Request], None]] = None):
+                 on_done: Optional[Callable[[Request], None]] = None, crossover_tris: Optional[int] = None):
         import ctypes as C
 
         import torch
@@ -135,6 +135,10 @@ class Server:
         self.scenes = scenes
         self.budget = int(budget_bytes)
         self.on_done = on_done
+        # autotune.batch_crossover: requests on scenes below it are traced by
+        # brute force, the others by the four-wide BVH (None: the request's own)
+        self.crossover_tris = crossover_tris
+        self.hitter_counts: Dict[str, int] = {}
         n = max(1, int(lanes))
         items, pool = max(1, int(max_items) // n), max(1, int(max_pool_rays) // n)
         self.engine_bytes = n * B.Batch.device_bytes(items, pool)
@@ -190,6 +194,11 @@ class Server:
             if sc is None:
                 return  # its scene fits only after requests in flight release theirs
             heapq.heappop(self.pending)
+            if self.crossover_tris is not None:
+                from .autotune import hitter_for
+
+                req.wl = req.wl.with_(hitter=hitter_for(int(sc.n_tris), int(self.crossover_tris)))
+            self.hitter_counts[req.wl.hitter] = self.hitter_counts.get(req.wl.hitter, 0) + 1
             # the new map is zeroed on the current stream; a large request goes
             # to every lane as disjoint ray ranges adding into that map (ray
             # ids are grid indices, so the map is the same as in one piece)

@@ -39,6 +39,28 @@ def test_brute_and_bvh_match_oracle(torch_cuda, subdiv, noise):
         assert np.array_equal(t.view(np.uint32), o_t.view(np.uint32)), f"hitter {hitter}: t bits differ"
 
 
+@pytest.mark.parametrize("tile", [32, 128])
+def test_brute_tile_sizes_match_oracle(torch_cuda, tile):
+    """The brute-force hitter with 32 and 128 hit records per ring stage
+    (SPLAT_TUNE_BRUTE_TILE) against the oracle, bit for bit."""
+    from splat_gb300 import _lib as L
+    from splat_gb300 import tracer
+
+    lib = L.load()
+    old = lib.splat_get_tuning(L.TUNE_BRUTE_TILE)
+    tris, fd = small_scene(3, 0.05)
+    scene = tracer.Scene(tris, fd, bvh=False)
+    rays = random_rays(5000, 17, tris.shape[0])
+    o_hit, o_t = O.next_hit(rays, tris)
+    try:
+        L.check(lib.splat_set_tuning(L.TUNE_BRUTE_TILE, tile))
+        hit, t = _hits(tracer, scene, tracer.BRUTE, rays)
+    finally:
+        L.check(lib.splat_set_tuning(L.TUNE_BRUTE_TILE, old))
+    assert np.array_equal(hit, o_hit)
+    assert np.array_equal(t.view(np.uint32), o_t.view(np.uint32))
+
+
 def test_ntris_dropin_matches_oracle(torch_cuda):
     from splat_gb300 import tracer
 
