@@ -96,14 +96,15 @@ def peaks():
     return {"hbm_gbs": PEAKS_FALLBACK["hbm_gbs"], "source": "fallback"}
 
 
-def profile_traffic(kernel: str):
-    """Per-launch DRAM bytes of a kernel from the committed ncu summary
-    (profiles/traffic.txt, lines 'kernel: bytes_per_launch ...')."""
+def profile_traffic(workload: str, kernel: str):
+    """Per-launch DRAM bytes of a kernel on a workload from the committed ncu
+    summary (profiles/traffic.txt, lines 'workload kernel: bytes_per_launch
+    ...')."""
     p = os.path.join(ROOT, "profiles", "traffic.txt")
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith(kernel + ":"):
+        if line.startswith(f"{workload} {kernel}:"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -368,10 +369,13 @@ def run_ours(args):
     bytes_per_launch = alg / n_kind_launches
     avg_launch_s = dom_ms / 1e3 / n_kind_launches
     achieved = bytes_per_launch / avg_launch_s / 1e9
-    kernel_name = {"hit_bvh": "hit_bvh_kernel" if wl.hitter == "bvh2" else "hit_bvh4_kernel",
+    packet = int(lib.splat_get_tuning(L.TUNE_BVH_PACKET))
+    bvh4_name = {0: "hit_bvh4_kernel", 1: "hit_bvh4_packet_kernel (bounce 1) + hit_bvh4_kernel",
+                 2: "hit_bvh4_packet_kernel"}.get(packet, "hit_bvh4_packet_kernel (per-warp packet choice)")
+    kernel_name = {"hit_bvh": "hit_bvh_kernel" if wl.hitter == "bvh2" else bvh4_name,
                    "hit_brute": "hit_brute_kernel", "evolve": "evolve_kernel",
                    "splat": "splat_kernel", "generate": "generate_soa_kernel"}[dom]
-    traffic = profile_traffic(kernel_name)
+    traffic = profile_traffic(args.workload, {"hit_bvh": "hit_bvh4", "hit_brute": "hit_brute"}.get(dom, dom))
     roofline = {"bound": "hbm", "achieved": round(achieved, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": round(achieved / pk["hbm_gbs"], 5), "traffic": traffic, "kernel": kernel_name,
                 "peak_source": pk["source"], "algorithmic_bytes_per_launch": round(bytes_per_launch),
@@ -818,10 +822,32 @@ def run_batched(args):
     cross = A.batch_crossover()
     eng = B.Lanes(2, frames, scenes, maps_batch, crossover_tris=cross["crossover_tris"])
     n_ticks = eng.capture()
+    old_persistent = int(lib.splat_get_tuning(L.TUNE_BATCH_PERSISTENT))
     tuned = A.tune_batch(eng, [w.seed for w in frames], reps=1, signature="batched-64-frames-seed5")
-    tuned_knobs = A.get_knobs(A.BATCH_KNOB_CHOICES)
-    knob_names = {L.TUNE_BVH_BLOCKS_PER_SM: "bvh_blocks_per_sm", L.TUNE_EVOLVE_BLOCKS_PER_SM: "evolve_blocks_per_sm",
-                  L.TUNE_SPLAT_BLOCKS_PER_SM: "splat_blocks_per_sm", L.TUNE_SPLAT_AGGREGATE: "splat_aggregate"}
+    tuned_knobs = A.get_knobs({**A.BATCH_KNOB_CHOICES, L.TUNE_BATCH_PERSISTENT: (0,)})
+
+    def time_replays(k0):
+        for k in range(W):
+            eng.replay([w.seed + 1000 * (k0 + k) for w in frames])
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for k in range(K):
+            eng.replay([w.seed + 1000 * (k0 + W + k) for w in frames])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / K
+
+    # both forms of the pass, whichever the tuner chose: tick by tick (five
+    # launches per tick in a graph) and one persistent launch per engine
+    forms = {}
+    for name, on in (("tick_by_tick", False), ("persistent", True)):
+        eng.persistent(on)
+        forms[name] = {"ms_per_pass": time_replays(100)}
+        # the maps of the last replay (seeds w.seed + 1000 (100 + W + K - 1)) against the plain loop's
+        plain_pass(100 + W + K - 1)
+        torch.cuda.synchronize()
+        forms[name]["maps_identical_to_plain_loop"] = all(torch.equal(a, b) for a, b in zip(maps_plain, maps_batch))
+    eng.persistent(bool(tuned_knobs.get(L.TUNE_BATCH_PERSISTENT, 0)))
     for k in range(W):
         eng.replay([w.seed + 1000 * k for w in frames])
     torch.cuda.synchronize()
@@ -831,6 +857,8 @@ def run_batched(args):
     e1.record(stream)
     torch.cuda.synchronize()
     batch_ms = e0.elapsed_time(e1) / K
+    plain_pass(W + K - 1)  # the plain loop's maps for the last replay's seeds
+    torch.cuda.synchronize()
     same = all(torch.equal(a, b) for a, b in zip(maps_plain, maps_batch))
     # the plain loop again under the tuned knobs (they reach its kernels too);
     # the faster of its two timings is the one compared against
@@ -846,6 +874,7 @@ def run_batched(args):
     plain_default_ms = plain_ms
     plain_ms = min(plain_ms, plain_tuned_ms)
     A.set_knobs(default_knobs)
+    L.check(lib.splat_set_tuning(L.TUNE_BATCH_PERSISTENT, old_persistent))
     from collections import Counter
 
     autotune = {"crossover_tris": cross["crossover_tris"],
@@ -853,7 +882,7 @@ def run_batched(args):
                                      "bvh_ms": round(r["ms"]["bvh"], 4)} for r in cross["rows"]],
                 "crossover_rays_per_frame": cross["n_rays"],
                 "hitters": dict(Counter(eng.hitters)),
-                "batch_knobs": {knob_names[k]: v for k, v in tuned_knobs.items()},
+                "batch_knobs": A.named(tuned_knobs),
                 "batch_knob_trials": tuned.get("trials"), "cache": A.cache_path()}
     out = {"metric": "batched frames/s", "value": 64 / (batch_ms / 1e3), "unit": "frames/s", "n_gpus": 1,
            "steps": K, "warmup": W, "ms_per_step": batch_ms, "higher_is_better": True, "scaling": "weak",
@@ -867,6 +896,10 @@ def run_batched(args):
                                     "ms_per_pass_tuned_knobs": plain_tuned_ms},
            "autotune": autotune,
            "speedup_vs_plain_loop": plain_ms / batch_ms, "maps_identical_to_plain_loop": bool(same),
+           "pass_forms": {k: {"ms_per_pass": round(v["ms_per_pass"], 4),
+                              "speedup_vs_plain_loop": round(plain_ms / v["ms_per_pass"], 4),
+                              "maps_identical_to_plain_loop": v["maps_identical_to_plain_loop"]}
+                          for k, v in forms.items()},
            "dropin_per_frame_loop": {
                "frames_per_s": 64 / (dropin_ms / 1e3), "ms_per_pass": dropin_ms,
                "api": "per frame: map zeroed, splat_rays_from_light, splat_run_evolution, splat_continuum_light_map "

@@ -515,7 +515,11 @@ enum {
                                             32, 64 (default) or 128 */
     SPLAT_TUNE_COUNT_WORK = 12,          /* four-wide BVH: 0 (default) plain kernels; 1 counting kernels that add
                                             their traversal work to counters read by splat_hit_work */
-    SPLAT_TUNE_KEYS = 13
+    SPLAT_TUNE_BATCH_PERSISTENT = 13,    /* splat_batch_capture: 0 (default) one tick at a time (five launches
+                                            per tick); k = 1..8 the whole pass as one persistent cooperative
+                                            launch over 1/k of the GPU's resident blocks (k engines replaying
+                                            side by side), grid-wide waits between its phases */
+    SPLAT_TUNE_KEYS = 14
 };
 splat_status_t splat_set_tuning(int32_t key, int32_t value);
 int32_t splat_get_tuning(int32_t key);

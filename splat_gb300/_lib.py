@@ -164,7 +164,8 @@ TUNE_TEST_WAIT_STALL = 9
 TUNE_RAY_ORDER = 10
 TUNE_BRUTE_TILE = 11
 TUNE_COUNT_WORK = 12
-TUNE_KEYS = 13
+TUNE_BATCH_PERSISTENT = 13
+TUNE_KEYS = 14
 
 KERNEL_GENERATE = 0
 KERNEL_HIT_BRUTE = 1

@@ -179,7 +179,7 @@ KNOB_NAMES = {L.TUNE_BRUTE_BLOCKS_PER_SM: "brute_blocks_per_sm", L.TUNE_BVH_BLOC
               L.TUNE_SPLAT_AGGREGATE: "splat_aggregate", L.TUNE_BVH_PACKET: "bvh_packet",
               L.TUNE_SPLAT_OVERLAP: "splat_overlap", L.TUNE_BVH_REFILL: "bvh_refill",
               L.TUNE_TRACE_SPLIT: "trace_split", L.TUNE_RAY_ORDER: "ray_order_bits",
-              L.TUNE_BRUTE_TILE: "brute_tile"}
+              L.TUNE_BRUTE_TILE: "brute_tile", L.TUNE_BATCH_PERSISTENT: "batch_persistent_share"}
 
 
 def named(knobs: Dict) -> Dict[str, int]:
@@ -279,10 +279,14 @@ def tune_batch(lanes, seeds: Sequence[int], reps: int = 2, use_cache: bool = Tru
         lanes.capture()
         return time_ms(lambda: lanes.replay(seeds), reps)
 
-    best, best_ms, trials = descend(BATCH_KNOB_CHOICES, get_knobs(BATCH_KNOB_CHOICES), cost)
+    # the pass tick by tick, or as one persistent launch per engine over its
+    # share of the GPU
+    choices = {**BATCH_KNOB_CHOICES, L.TUNE_BATCH_PERSISTENT: (0, len(lanes.engines))}
+    best, best_ms, trials = descend(choices, get_knobs(choices), cost)
     set_knobs(best)
     lanes.capture()
-    out = {"knobs": {str(k): v for k, v in best.items()}, "ms": best_ms, "trials": len(trials)}
+    out = {"knobs": {str(k): v for k, v in best.items()}, "ms": best_ms, "trials": len(trials),
+           "trial_ms": [(named(k), round(c, 4)) for k, c in trials]}
     if use_cache and key:
         cache_put(key, out)
     return out

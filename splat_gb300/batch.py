@@ -151,7 +151,21 @@ class Lanes:
             self.engines.append(eng)
 
     def capture(self) -> int:
+        """Captures every engine's pass; with SPLAT_TUNE_BATCH_PERSISTENT set
+        each pass is one persistent launch (see persistent())."""
         return max(e.capture() for e in self.engines)
+
+    def persistent(self, on: bool = True) -> int:
+        """Re-captures the passes as persistent launches (each engine over
+        1/n_lanes of the GPU, so the lanes' launches run side by side) or,
+        with on=False, tick by tick; returns the ticks per pass."""
+        lib = L.load()
+        old = lib.splat_get_tuning(L.TUNE_BATCH_PERSISTENT)
+        L.check(lib.splat_set_tuning(L.TUNE_BATCH_PERSISTENT, len(self.engines) if on else 0))
+        try:
+            return self.capture()
+        finally:
+            L.check(lib.splat_set_tuning(L.TUNE_BATCH_PERSISTENT, old))
 
     def replay(self, seeds: Optional[Sequence[int]] = None) -> None:
         """seeds: one per frame, in the order the frames were given."""

@@ -1025,6 +1025,8 @@ splat_status_t splat_set_tuning(int32_t key, int32_t value) {
         if (value < 0 || value > 32) return fail(SPLAT_ERR_INVALID, "set_tuning: refill threshold must be 0..32");
     } else if (key == SPLAT_TUNE_TRACE_SPLIT) {
         if (value < 1 || value > kMaxTraceParts) return fail(SPLAT_ERR_INVALID, "set_tuning: split must be 1..4");
+    } else if (key == SPLAT_TUNE_BATCH_PERSISTENT) {
+        if (value < 0 || value > 8) return fail(SPLAT_ERR_INVALID, "set_tuning: persistent pass share must be 0..8");
     } else if (key == SPLAT_TUNE_COUNT_WORK) {
         if (value != 0 && value != 1) return fail(SPLAT_ERR_INVALID, "set_tuning: count work must be 0 or 1");
     } else if (key == SPLAT_TUNE_BRUTE_TILE) {
@@ -1290,6 +1292,54 @@ splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done
     return SPLAT_OK;
 }
 
+// Counters of a persistent pass in the batch's counter block (int64 slots).
+constexpr int kPassCount = 16, kPassQCount = 26, kPassQMark = 28, kPassFetch = 40, kPassSplatFetch = 50,
+              kPassBar = 60, kPassEnd = 64;
+
+// Every tick from b->tick to `last` as one persistent launch over 1/share of
+// the GPU (items all start at b->tick); the host bookkeeping advances as the
+// tick-by-tick path would.
+cudaError_t batch_enqueue_pass(splat_batch* b, cudaStream_t st, int32_t last, int share) {
+    const int32_t t0 = b->tick;
+    int32_t kind = -2;
+    for (int32_t s = 0; s < b->max_items; ++s) {
+        if (!b->used[(size_t)s] || b->start[(size_t)s] + b->depth[(size_t)s] - 1 < t0) continue;
+        kind = kind == -2 || kind == b->mat_kind[(size_t)s] ? b->mat_kind[(size_t)s] : -1;
+        if (b->start[(size_t)s] == t0 && b->zero_map[(size_t)s]) {
+            cudaError_t e = cudaMemsetAsync(b->maps[(size_t)s], 0, b->map_bytes[(size_t)s], st);
+            if (e != cudaSuccess) return e;
+        }
+    }
+    cudaError_t e = cudaMemsetAsync(&b->counts[kPassCount], 0, sizeof(int64_t) * (kPassEnd - kPassCount), st);
+    if (e != cudaSuccess) return e;
+    BatchPassArgs a;
+    a.items = b->d_items;
+    a.fresh = b->d_fresh;
+    a.n_slots = b->max_items;
+    a.t0 = t0;
+    a.n_ticks = last - t0 + 1;
+    a.material_kind = kind < 0 ? -1 : kind;
+    a.a = b->parity ? b->b : b->a;
+    a.b = b->parity ? b->a : b->b;
+    a.queue = b->q;
+    a.count = &b->counts[kPassCount];
+    a.qcount = &b->counts[kPassQCount];
+    a.qmark = &b->counts[kPassQMark];
+    a.fetch = reinterpret_cast<unsigned long long*>(&b->counts[kPassFetch]);
+    a.splat_fetch = reinterpret_cast<unsigned long long*>(&b->counts[kPassSplatFetch]);
+    a.bar = reinterpret_cast<unsigned*>(&b->counts[kPassBar]);
+    a.hit_idx = b->hit;
+    a.err = b->d_err;
+    {
+        ProfScope ps(SPLAT_KERNEL_BATCH, st);
+        e = launch_batch_pass(a, share, sm_count_current(), st);
+        if (e != cudaSuccess) return e;
+    }
+    b->tick = last + 1;
+    b->parity ^= a.n_ticks & 1;
+    return cudaSuccess;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1488,10 +1538,18 @@ splat_status_t splat_batch_capture(splat_batch_t* b, void* stream, int32_t* n_ti
     cudaGraph_t graph = nullptr;
     b->overlap = g_tune[SPLAT_TUNE_SPLAT_OVERLAP] > 0 && batch_overlap_ready(b) == cudaSuccess;
     b->splat_pending[0] = b->splat_pending[1] = false;
+    const int persistent = g_tune[SPLAT_TUNE_BATCH_PERSISTENT].load();
+    if (persistent > 0 && last - t0 + 1 > kMaxPassTicks)
+        return fail(SPLAT_ERR_INVALID, "batch_capture: a persistent pass holds at most 8 ticks");
+    if (persistent > 0) b->overlap = false;
     SPLAT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "batch_capture: begin");
     cudaError_t e = cudaMemsetAsync(&b->counts[p0], 0, sizeof(int64_t), st);
     rc = SPLAT_OK;
-    while (e == cudaSuccess && rc == SPLAT_OK && b->tick <= last) rc = batch_enqueue_tick(b, st, nullptr, 0, nullptr);
+    if (persistent > 0) {
+        if (e == cudaSuccess) e = batch_enqueue_pass(b, st, last, persistent);
+    } else {
+        while (e == cudaSuccess && rc == SPLAT_OK && b->tick <= last) rc = batch_enqueue_tick(b, st, nullptr, 0, nullptr);
+    }
     for (int p = 0; p < 2 && e == cudaSuccess; ++p)
         if (b->overlap && b->splat_pending[p]) {
             e = cudaStreamWaitEvent(st, b->splat_ev[p], 0);  // join the side stream before the capture ends

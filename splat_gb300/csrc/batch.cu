@@ -65,11 +65,14 @@ struct FreshList {
     int64_t offset[kMaxBatchItems];
 };
 
+// Phase bodies of a tick, shared by the per-tick kernels and the persistent
+// pass kernel: each takes its block index and block count.
+
 // The items starting this tick, in slot order, get consecutive pool ranges
 // after the survivors: one thread per slot, block-wide exclusive scans of
-// (starts, rays).
-__global__ void __launch_bounds__(kMaxBatchItems) batch_reserve_kernel(const BatchItem* items, int n_slots, int tick,
-                                                                       int64_t* cur_count, FreshList* fresh) {
+// (starts, rays).  One block of kMaxBatchItems threads.
+__device__ __forceinline__ void reserve_phase(const BatchItem* items, int n_slots, int tick, int64_t* cur_count,
+                                              FreshList* fresh) {
     __shared__ int s_wcount[kMaxBatchItems / 32];
     __shared__ long long s_wrays[kMaxBatchItems / 32];
     const int s = threadIdx.x;
@@ -112,11 +115,17 @@ __global__ void __launch_bounds__(kMaxBatchItems) batch_reserve_kernel(const Bat
     }
 }
 
-__global__ void batch_generate_kernel(const BatchItem* __restrict__ items, const FreshList* __restrict__ fresh,
-                                      RaySoA out) {
+__global__ void __launch_bounds__(kMaxBatchItems) batch_reserve_kernel(const BatchItem* items, int n_slots, int tick,
+                                                                       int64_t* cur_count, FreshList* fresh) {
+    reserve_phase(items, n_slots, tick, cur_count, fresh);
+}
+
+__device__ __forceinline__ void generate_phase(const BatchItem* __restrict__ items,
+                                               const FreshList* __restrict__ fresh, RaySoA out, int64_t bid,
+                                               int64_t nblk) {
     const int64_t total = fresh->total;
     const int nf = fresh->n;
-    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t g = bid * blockDim.x + threadIdx.x; g < total; g += nblk * blockDim.x) {
         int lo = 0, hi = nf - 1;
         while (lo < hi) {  // last f with prefix[f] <= g
             const int mid = (lo + hi + 1) >> 1;
@@ -131,10 +140,15 @@ __global__ void batch_generate_kernel(const BatchItem* __restrict__ items, const
     }
 }
 
+__global__ void batch_generate_kernel(const BatchItem* __restrict__ items, const FreshList* __restrict__ fresh,
+                                      RaySoA out) {
+    generate_phase(items, fresh, out, blockIdx.x, gridDim.x);
+}
+
 template <bool ANY_BRUTE>
-__global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t* __restrict__ count,
-                                                        const BatchItem* __restrict__ items, int32_t* hit_idx,
-                                                        int32_t* err, unsigned long long* fetch) {
+__device__ __forceinline__ void hit_phase(RaySoA in, const int64_t* __restrict__ count,
+                                          const BatchItem* __restrict__ items, int32_t* hit_idx, int32_t* err,
+                                          unsigned long long* fetch) {
     const int64_t n = *count;
     int2 stack[kBvhStack];
     RaySrc src{};
@@ -154,17 +168,23 @@ __global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t
     });
 }
 
+template <bool ANY_BRUTE>
+__global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t* __restrict__ count,
+                                                        const BatchItem* __restrict__ items, int32_t* hit_idx,
+                                                        int32_t* err, unsigned long long* fetch) {
+    hit_phase<ANY_BRUTE>(in, count, items, hit_idx, err, fetch);
+}
+
 constexpr int kBatchThreads = 256;
 
 // MK >= 0: every item in flight has this material kind (compile-time, so
-// only its optics is inlined); -1: per item.
+// only its optics is inlined); -1: per item.  Whole blocks of kBatchThreads.
 template <int MK>
-__global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, RaySoA out, RaySoA queue,
-                                                                     const int64_t* __restrict__ in_count,
-                                                                     int64_t* out_count, int64_t* queue_count,
-                                                                     const BatchItem* __restrict__ items, int tick,
-                                                                     const int32_t* __restrict__ hit_idx,
-                                                                     int32_t* err) {
+__device__ __forceinline__ void evolve_phase(RaySoA in, RaySoA out, RaySoA queue, const int64_t* __restrict__ in_count,
+                                             int64_t* out_count, int64_t* queue_count,
+                                             const BatchItem* __restrict__ items, int tick,
+                                             const int32_t* __restrict__ hit_idx, int32_t* err, int64_t bid,
+                                             int64_t nblk) {
     // double-buffered by iteration parity, as in evolve_kernel
     __shared__ int s_keep2[2][kBatchThreads / 32], s_dif2[2][kBatchThreads / 32];
     __shared__ unsigned long long s_kbase2[2], s_dbase2[2];
@@ -172,8 +192,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, 
     const int lane = lane_id();
     const int wid = threadIdx.x >> 5;
     int par = 0;
-    for (int64_t base = (int64_t)blockIdx.x * kBatchThreads; base < n;
-         base += (int64_t)gridDim.x * kBatchThreads, par ^= 1) {
+    for (int64_t base = bid * kBatchThreads; base < n; base += nblk * kBatchThreads, par ^= 1) {
         int* s_keep = s_keep2[par];
         int* s_dif = s_dif2[par];
         unsigned long long& s_kbase = s_kbase2[par];
@@ -222,21 +241,35 @@ __global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, 
     }
 }
 
+template <int MK>
+__global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, RaySoA out, RaySoA queue,
+                                                                     const int64_t* __restrict__ in_count,
+                                                                     int64_t* out_count, int64_t* queue_count,
+                                                                     const BatchItem* __restrict__ items, int tick,
+                                                                     const int32_t* __restrict__ hit_idx,
+                                                                     int32_t* err) {
+    evolve_phase<MK>(in, out, queue, in_count, out_count, queue_count, items, tick, hit_idx, err, blockIdx.x,
+                     gridDim.x);
+}
+
 // One lane per queued ray, walking all of its planes: rays of one item are
 // adjacent in the queue, so a warp's lanes usually share an item and its
 // plane count, and no lane idles on frames with few planes.
+__device__ __forceinline__ void splat_one(RaySoA q, int64_t k, const BatchItem* __restrict__ items) {
+    const RayState r = load_ray(q, k);
+    const BatchItem& it = items[q.id[k] >> kSlotShift];
+    const SplatView sp = splat_view(it.sp);
+    const int planes = sp.n_lambda > 0 ? sp.n_lambda : 1;
+    const Tri T = load_tri(it.ftri, r.ignore);
+    const TriUV quv = tri_uv(T);
+    for (int il = 0; il < planes; ++il) (void)splat_ray_plane(sp, r, T, quv, il);
+}
+
 __global__ void __launch_bounds__(256, 2) batch_splat_kernel(RaySoA q, const int64_t* __restrict__ count,
                                                              const BatchItem* __restrict__ items) {
     const int64_t n = *count;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-        const RayState r = load_ray(q, k);
-        const BatchItem& it = items[q.id[k] >> kSlotShift];
-        const SplatView sp = splat_view(it.sp);
-        const int planes = sp.n_lambda > 0 ? sp.n_lambda : 1;
-        const Tri T = load_tri(it.ftri, r.ignore);
-        const TriUV quv = tri_uv(T);
-        for (int il = 0; il < planes; ++il) (void)splat_ray_plane(sp, r, T, quv, il);
-    }
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        splat_one(q, k, items);
 }
 
 // The same through the block's shared texel table keyed by texel address
@@ -275,6 +308,113 @@ __global__ void __launch_bounds__(256, 2) batch_splat_agg_kernel(RaySoA q, const
             addr_table_flush(s_key, s_val);
             __syncthreads();
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// persistent pass: every tick of a captured pass in one cooperative launch
+// ---------------------------------------------------------------------------
+// All items start at the pass's first tick.  Per tick: reserve (block 0) |
+// generate | this tick's traversal, then the previous tick's splat segment
+// (warps take 32 rays at a time from work counters, so the blocks done with
+// the traversal splat while its last rays are traced) | evolve, with a
+// bounded grid-wide wait between the phases.  The splat queue fills over the
+// whole pass (a ray is queued at most once, so the pool's capacity holds
+// it); tick i's segment is [qmark[i], qmark[i + 1]).
+constexpr uint32_t kGridWaitLimit = 1u << 22;  // polls of >= 256 ns: over a second
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide wait: every block arrives, then waits until `target` arrivals,
+// at most kGridWaitLimit polls; gives up with error bit 64 (no trap, no
+// unbounded spin).  The fences make every block's writes before the wait
+// visible to every block after it.
+__device__ __forceinline__ bool grid_wait(unsigned* bar, unsigned target, int32_t* err) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(bar, 1u);
+        int ok = 1;
+        for (uint32_t it = 0; ld_acquire(bar) < target; ++it) {
+            if (it >= kGridWaitLimit) {
+                atomicOr(err, 64);
+                ok = 0;
+                break;
+            }
+            __nanosleep(256);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <int MK>
+__global__ void __launch_bounds__(kBatchThreads, 2) batch_pass_kernel(BatchPassArgs P) {
+    const BatchItem* items = reinterpret_cast<const BatchItem*>(P.items);
+    FreshList* fresh = reinterpret_cast<FreshList*>(P.fresh);
+    const unsigned nblk = gridDim.x;
+    unsigned waits = 0;
+    for (int i = 0; i < P.n_ticks; ++i) {
+        const int tick = P.t0 + i;
+        const RaySoA cur = (i & 1) ? P.b : P.a, nxt = (i & 1) ? P.a : P.b;
+        if (blockIdx.x == 0) {
+            reserve_phase(items, P.n_slots, tick, &P.count[i], fresh);
+            if (threadIdx.x == 0) P.qmark[i] = *P.qcount;  // the queue before this tick's evolve
+        }
+        if (!grid_wait(P.bar, ++waits * nblk, P.err)) return;
+        generate_phase(items, fresh, cur, blockIdx.x, nblk);
+        if (!grid_wait(P.bar, ++waits * nblk, P.err)) return;
+        hit_phase<true>(cur, &P.count[i], items, P.hit_idx, P.err, &P.fetch[i]);
+        if (i > 0) {
+            const int64_t q0 = P.qmark[i - 1], q1 = P.qmark[i];
+            for_each_ray(q1 - q0, &P.splat_fetch[i - 1], [&](int64_t k) { splat_one(P.queue, q0 + k, items); });
+        }
+        if (!grid_wait(P.bar, ++waits * nblk, P.err)) return;
+        evolve_phase<MK>(cur, nxt, P.queue, &P.count[i], &P.count[i + 1], P.qcount, items, tick, P.hit_idx, P.err,
+                         blockIdx.x, nblk);
+        if (!grid_wait(P.bar, ++waits * nblk, P.err)) return;
+    }
+    const int64_t q0 = P.qmark[P.n_ticks - 1], q1 = *P.qcount;
+    for_each_ray(q1 - q0, &P.splat_fetch[P.n_ticks - 1], [&](int64_t k) { splat_one(P.queue, q0 + k, items); });
+}
+
+template <int MK>
+static cudaError_t launch_pass_mk(const BatchPassArgs& a, int share, int sm_count, cudaStream_t s) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_pass_kernel<MK>, kBatchThreads, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    int grid = per_sm * sm_count / (share < 1 ? 1 : share);
+    if (grid < 1) grid = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kBatchThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, batch_pass_kernel<MK>, a);
+    ++g_launches;
+    return e;
+}
+
+cudaError_t launch_batch_pass(const BatchPassArgs& a, int share, int sm_count, cudaStream_t s) {
+    if (a.n_ticks < 1 || a.n_ticks > kMaxPassTicks) return cudaErrorInvalidValue;
+    switch (a.material_kind) {
+        case SPLAT_MATERIAL_LINEAR_REF: return launch_pass_mk<SPLAT_MATERIAL_LINEAR_REF>(a, share, sm_count, s);
+        case SPLAT_MATERIAL_CAUCHY: return launch_pass_mk<SPLAT_MATERIAL_CAUCHY>(a, share, sm_count, s);
+        case SPLAT_MATERIAL_SELLMEIER: return launch_pass_mk<SPLAT_MATERIAL_SELLMEIER>(a, share, sm_count, s);
+        default: return launch_pass_mk<-1>(a, share, sm_count, s);
     }
 }
 

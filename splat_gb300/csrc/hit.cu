@@ -24,7 +24,7 @@
 namespace splat {
 
 thread_local int64_t g_launches = 0;
-std::atomic<int32_t> g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1, 2, 0, 2, 0, 0, 64, 0};
+std::atomic<int32_t> g_tune[SPLAT_TUNE_KEYS] = {4, 16, 8, 8, 0, 1, 2, 0, 2, 0, 0, 64, 0, 0};
 
 // ---------------------------------------------------------------------------
 // PTX helpers: mbarrier + bulk copy (sm_90+ async proxy)

@@ -261,6 +261,27 @@ struct BatchTickArgs {
 };
 
 cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s);
+
+// A whole pass (ticks t0 .. t0 + n_ticks - 1 of items that all start at t0)
+// as one persistent cooperative launch over 1/share of the GPU's resident
+// blocks; every counter below is zeroed by the caller before the launch.
+constexpr int kMaxPassTicks = 8;
+struct BatchPassArgs {
+    void* items;
+    void* fresh;
+    int n_slots, t0, n_ticks;
+    int material_kind;   // shared by every item, -1 when mixed
+    RaySoA a, b, queue;  // a: the first tick's rays
+    int64_t* count;      // count[i]: rays entering tick t0 + i (n_ticks + 1 slots)
+    int64_t* qcount;     // queue entries so far
+    int64_t* qmark;      // qmark[i]: queue length before tick i's evolve (n_ticks slots)
+    unsigned long long* fetch;        // per-tick traversal work counters (n_ticks)
+    unsigned long long* splat_fetch;  // per-tick splat work counters (n_ticks)
+    unsigned* bar;       // grid-wait arrivals
+    int32_t* hit_idx;
+    int32_t* err;
+};
+cudaError_t launch_batch_pass(const BatchPassArgs& a, int share, int sm_count, cudaStream_t s);
 // the two halves of a tick: reserve, generate, hit, evolve; and the splat of the tick's queue
 cudaError_t launch_batch_trace(const BatchTickArgs& a, cudaStream_t s);
 cudaError_t launch_batch_splat(const BatchTickArgs& a, cudaStream_t s);

@@ -28,7 +28,9 @@ def tmp_cache(tmp_path, monkeypatch):
 def restore_knobs(torch_cuda):
     from splat_gb300 import autotune as A
 
-    old = A.get_knobs()
+    from splat_gb300 import _lib as L
+
+    old = {**A.get_knobs(), **A.get_knobs({L.TUNE_BATCH_PERSISTENT: (0,)})}
     yield
     A.set_knobs(old)
 
@@ -69,7 +71,9 @@ def test_tuned_hitters_and_batch_knobs_keep_every_map(torch_cuda, restore_knobs)
     assert lanes.hitters == ["brute", "brute", "bvh", "bvh"]
     seeds = [w.seed for w in wls]
     tuned = A.tune_batch(lanes, seeds, reps=1, use_cache=False)
-    assert set(tuned["knobs"]) == {str(k) for k in A.BATCH_KNOB_CHOICES}
+    from splat_gb300 import _lib as L
+
+    assert set(tuned["knobs"]) == {str(k) for k in A.BATCH_KNOB_CHOICES} | {str(L.TUNE_BATCH_PERSISTENT)}
     lanes.replay(seeds)
     for (sc, wl), m in zip(fr, maps):
         alone = tracer.trace_forward(wl, scene=sc).tex

@@ -157,3 +157,29 @@ def test_lanes_replay_concurrently_and_equal_alone(frames):
         lanes.replay(seeds)
         for i, (sc, wl) in enumerate(frames):
             _check(wl, maps[i].cpu().numpy(), _alone(sc, wl, seeds[i]), f"frame {i} pass {k}")
+
+
+@pytest.mark.parametrize("n_lanes", [1, 2])
+def test_persistent_pass_equals_alone(frames, n_lanes):
+    """The captured pass as one persistent cooperative launch per engine
+    (SPLAT_TUNE_BATCH_PERSISTENT; grid-wide waits between reserve, generate,
+    traversal + the previous tick's splat, evolve): every map equals the
+    frame's alone result, pass after pass, and re-capturing tick by tick
+    gives the same maps again."""
+    from splat_gb300 import batch, tracer
+
+    scenes = [sc for sc, _ in frames]
+    wls = [wl for _, wl in frames]
+    maps = [tracer.new_light_map(w.map_w, w.map_h, w.n_planes, w.accum) for w in wls]
+    lanes = batch.Lanes(n_lanes, wls, scenes, maps)
+    n_ticks = lanes.persistent(True)
+    assert n_ticks == max(w.depth for w in wls)
+    for k in range(2):
+        seeds = [w.seed + 11 * k for w in wls]
+        lanes.replay(seeds)
+        for i, (sc, wl) in enumerate(frames):
+            _check(wl, maps[i].cpu().numpy(), _alone(sc, wl, seeds[i]), f"frame {i} pass {k}")
+    lanes.persistent(False)
+    lanes.replay([w.seed for w in wls])
+    for i, (sc, wl) in enumerate(frames):
+        _check(wl, maps[i].cpu().numpy(), _alone(sc, wl), f"frame {i} tick by tick")
