@@ -77,6 +77,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default knobs (no autotuning)")
     ap.add_argument("--no-secondary", action="store_true", help="headline workload only")
+    ap.add_argument("--knobs", default=None,
+                    help='JSON of knobs by name to set instead of autotuning, e.g. {"ray_order_bits": 20}')
+    ap.add_argument("--light-res", type=int, default=0,
+                    help="profiling only: light grid side (fewer rays than the workload; reported in config)")
     return ap.parse_args()
 
 
@@ -252,6 +256,8 @@ def run_ours(args):
     torch.cuda.set_device(local)
     lib = L.load()
     wl = WORKLOADS[args.workload]()
+    if args.light_res:
+        wl = wl.with_(light=S.scaled_light(wl.light, args.light_res), name=wl.name + f"-light{args.light_res}")
     step = tracer.TraceStep(wl)
     stream = torch.cuda.current_stream()
     K, W = args.steps, args.warmup
@@ -261,7 +267,10 @@ def run_ours(args):
     from splat_gb300 import autotune as A
 
     default_knobs = A.get_knobs()
-    tuned = None if args.no_tune else A.tune_knobs(step, reps=3, use_cache=False)
+    if args.knobs:
+        by_name = {v: k for k, v in A.KNOB_NAMES.items()}
+        A.set_knobs({by_name[k]: int(v) for k, v in json.loads(args.knobs).items()})
+    tuned = None if (args.no_tune or args.knobs) else A.tune_knobs(step, reps=3, use_cache=False)
     stats = torch.zeros((K, 16), dtype=torch.int64, device="cuda")
     base_seed = wl.seed + 1000003 * rank
 

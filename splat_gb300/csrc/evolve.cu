@@ -23,10 +23,7 @@
 namespace splat {
 
 constexpr unsigned kFull = 0xffffffffu;
-#ifndef SPLAT_EVOLVE_THREADS
-#define SPLAT_EVOLVE_THREADS 256
-#endif
-constexpr int kEvolveThreads = SPLAT_EVOLVE_THREADS;
+constexpr int kEvolveThreads = 256;
 
 __device__ __forceinline__ F3 shfl3(F3 v, int src) {
     return {__shfl_sync(kFull, v.x, src), __shfl_sync(kFull, v.y, src), __shfl_sync(kFull, v.z, src)};

@@ -105,16 +105,32 @@ __device__ __forceinline__ float comp(const float4& v, int i) {
     return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
+// Three-input min / max (one instruction each on sm_100 and later; the same
+// IEEE minNum / maxNum rule as the nested two-input forms).
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 // Entry and exit distances of a ray through the four child boxes of a
 // node.  The slab planes are picked by the signs of the inverse direction
 // (ix < 0: the near x plane is hi, else lo), through the addresses of the
 // node's per-axis float4s, so the test needs no per-axis min / max: each
 // distance is the one min(a, b) / max(a, b) of the two planes would pick,
 // bit for bit (lo <= hi for every real child; the empty slots, lo = +inf and
-// hi = -inf, come out with tmin > tmax, and the child count rejects them
-// anyway).
+// hi = -inf, come out with t0 > tmax, and the child count rejects them
+// anyway).  t0 is the entry distance clamped at the origin, max(tmin, 0):
+// for non-NaN values (tmin <= tmax and tmax >= 0) is t0 <= tmax, and, as
+// every accepted hit has t > 0, tmin <= best is t0 <= best, so a child is
+// entered exactly when the unclamped test enters it.
 __device__ __forceinline__ void node4_slabs(const Bvh4Node* nd, float ix, float iy, float iz, float oix, float oiy,
-                                            float oiz, float tmin[4], float tmax[4]) {
+                                            float oiz, float t0[4], float tmax[4]) {
     const float4* q = reinterpret_cast<const float4*>(nd);  // lox, hix, loy, hiy, loz, hiz
     const int sx = ix < 0.0f ? 1 : 0, sy = iy < 0.0f ? 1 : 0, sz = iz < 0.0f ? 1 : 0;
     const float4 nx = __ldg(q + sx), fx = __ldg(q + 1 - sx);
@@ -122,8 +138,9 @@ __device__ __forceinline__ void node4_slabs(const Bvh4Node* nd, float ix, float 
     const float4 nz = __ldg(q + 4 + sz), fz = __ldg(q + 5 - sz);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        tmin[i] = fmaxf(fmaxf(fmaf(comp(nx, i), ix, -oix), fmaf(comp(ny, i), iy, -oiy)), fmaf(comp(nz, i), iz, -oiz));
-        tmax[i] = fminf(fminf(fmaf(comp(fx, i), ix, -oix), fmaf(comp(fy, i), iy, -oiy)), fmaf(comp(fz, i), iz, -oiz));
+        t0[i] = max3f(fmaf(comp(nx, i), ix, -oix), fmaf(comp(ny, i), iy, -oiy),
+                      fmaxf(fmaf(comp(nz, i), iz, -oiz), 0.0f));
+        tmax[i] = min3f(fmaf(comp(fx, i), ix, -oix), fmaf(comp(fy, i), iy, -oiy), fmaf(comp(fz, i), iz, -oiz));
     }
 }
 
@@ -163,7 +180,7 @@ __device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bv
             node4_slabs(nd, ix, iy, iz, oix, oiy, oiz, tmin, tmax);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const bool h = (i < nc) & (tmin[i] <= tmax[i]) & (tmax[i] >= 0.0f) & (tmin[i] <= best);
+                const bool h = (i < nc) & (tmin[i] <= tmax[i]) & (tmin[i] <= best);  // tmin: clamped at 0
                 key[i] = h ? fminf(tmin[i], kMax) : kInf;
             }
             float k0 = key[0], k1 = key[1], k2 = key[2], k3 = key[3];
@@ -287,7 +304,7 @@ __device__ __forceinline__ void bvh4_refill_loop(int64_t n, unsigned long long* 
             node4_slabs(nd, ix, iy, iz, oix, oiy, oiz, tmin, tmax);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const bool h = (i < nc) & (tmin[i] <= tmax[i]) & (tmax[i] >= 0.0f) & (tmin[i] <= best);
+                const bool h = (i < nc) & (tmin[i] <= tmax[i]) & (tmin[i] <= best);  // tmin: clamped at 0
                 key[i] = h ? fminf(tmin[i], kMax) : kInf;
             }
             float k0 = key[0], k1 = key[1], k2 = key[2], k3 = key[3];
@@ -376,12 +393,10 @@ __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid,
             unsigned u[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                // t0 = max(tmin, 0): (tmin <= tmax and tmax >= 0) is t0 <= tmax, and
-                // tmin <= best is t0 <= best (best > 0: accepted hits have t > 0).
-                // Non-negative floats order as their bits, so t0's bits are the
-                // sort key (a -0 from the max sorts last: order only, never which
-                // children are entered)
-                const float t0 = fmaxf(tmin[i], 0.0f);
+                // tmin is clamped at 0 (node4_slabs): non-negative floats order as
+                // their bits, so its bits are the sort key (a -0 from the max sorts
+                // last: order only, never which children are entered)
+                const float t0 = tmin[i];
                 const bool h = valid & (i < nc) & (t0 <= tmax[i]) & (t0 <= best);
                 u[i] = __reduce_min_sync(0xffffffffu, h ? __float_as_uint(t0) : 0xffffffffu);
             }
