@@ -508,7 +508,7 @@ enum {
                                             polls), so each block takes the failure path of its bounded waits:
                                             error bit 1, bounded drain of its copies in flight, early return */
     SPLAT_TUNE_RAY_ORDER = 10,           /* fused trace step, four-wide BVH: 0 secondary rays traced in compaction
-                                            order; 4..20 each bounce after the first groups its rays by (direction
+                                            order; 4..22 each bounce after the first groups its rays by (direction
                                             octant, BVH position of the triangle they leave), a key of that many
                                             bits, before the hit launch (default 0) */
     SPLAT_TUNE_BRUTE_TILE = 11,          /* brute-force hitter: hit records per stage of its shared-memory ring,

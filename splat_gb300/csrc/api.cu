@@ -1033,8 +1033,8 @@ splat_status_t splat_set_tuning(int32_t key, int32_t value) {
         if (value != 32 && value != 64 && value != 128)
             return fail(SPLAT_ERR_INVALID, "set_tuning: brute tile must be 32, 64 or 128");
     } else if (key == SPLAT_TUNE_RAY_ORDER) {
-        if (value != 0 && (value < 4 || value > 20))
-            return fail(SPLAT_ERR_INVALID, "set_tuning: ray order bits must be 0 or 4..20");
+        if (value != 0 && (value < 4 || value > 22))
+            return fail(SPLAT_ERR_INVALID, "set_tuning: ray order bits must be 0 or 4..22");
     } else if (key == SPLAT_TUNE_TEST_WAIT_STALL) {
         if (value < 0 || value > (1 << 20)) return fail(SPLAT_ERR_INVALID, "set_tuning: stall tile must be 0..2^20");
     } else if (value < 1 || value > 256) {

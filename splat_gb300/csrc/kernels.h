@@ -103,7 +103,7 @@ cudaError_t launch_lbvh_build(const splat_ftri_t* ftri, int64_t n_tris, int leaf
 // Coherent ray order (lbvh.cu): a permutation of the d_count active rays of
 // a SoA bounce buffer, grouped by (direction octant, BVH-order position of
 // the triangle the ray leaves) with a counting sort over a key of key_bits
-// (4..20) bits (the position's low bits dropped to fit).  Rays that leave
+// (4..22) bits (the position's low bits dropped to fit).  Rays that leave
 // neighbouring triangles in similar directions then share warps, so the
 // traversal's lanes take similar paths.  bvh_pos[i]: BVH record position of
 // reference index i (0 for indices outside 1..n_tris).  *perm_out points

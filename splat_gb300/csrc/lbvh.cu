@@ -556,16 +556,25 @@ cudaError_t launch_lbvh_build(const splat_ftri_t* ftri, int64_t n_tris, int leaf
 // warp (__match_any_sync), so a warp's rays of one bucket stay together.
 // The order inside a bucket is the atomics' order: only which rays share a
 // warp changes with it, never a result.
-constexpr int kOrderMaxBits = 20;
+constexpr int kOrderMaxBits = 22;
+#ifdef SPLAT_ORDER_MAJOR
+constexpr int kDirClasses = 24, kDirBits = 5;  // octant x the largest |component|'s axis
+#else
+constexpr int kDirClasses = 8, kDirBits = 3;   // octant
+#endif
 
 __device__ __forceinline__ uint32_t ray_key(const float* __restrict__ f, int64_t cap, const int32_t* __restrict__ ignore,
                                             const int32_t* __restrict__ bvh_pos, int64_t n_tris, int pos_shift,
                                             uint32_t n_pos, int64_t k) {
-    const uint32_t oct = (f[3 * cap + k] < 0.0f ? 1u : 0u) | (f[4 * cap + k] < 0.0f ? 2u : 0u) |
-                         (f[5 * cap + k] < 0.0f ? 4u : 0u);
+    const float dx = f[3 * cap + k], dy = f[4 * cap + k], dz = f[5 * cap + k];
+    uint32_t cls = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
+    if (kDirClasses == 24) {
+        const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+        cls = cls * 3u + (ax >= ay && ax >= az ? 0u : (ay >= az ? 1u : 2u));
+    }
     const int32_t ig = ignore[k];
     const uint32_t pos = (ig >= 1 && (int64_t)ig <= n_tris) ? (uint32_t)bvh_pos[ig] : 0u;
-    return oct * n_pos + (pos >> pos_shift);
+    return cls * n_pos + (pos >> pos_shift);
 }
 
 // Bucket sizes: one atomic per group of equal keys in a warp.
@@ -627,10 +636,10 @@ cudaError_t launch_ray_order(const float* soa_f, const int32_t* ignore, int64_t 
     // positions 0 .. n_tris - 2 (the records); keep the high bits that fit
     int full_bits = 1;
     while (full_bits < 31 && (int64_t(1) << full_bits) < n_tris + 1) ++full_bits;
-    const int pos_bits = full_bits < key_bits - 3 ? full_bits : key_bits - 3;
+    const int pos_bits = full_bits < key_bits - kDirBits ? full_bits : key_bits - kDirBits;
     const int pos_shift = full_bits - pos_bits;
     const uint32_t n_pos = (uint32_t)((n_tris >> pos_shift) + 1);  // positions after the shift, all < n_pos
-    const int64_t buckets = 8 * (int64_t)n_pos;                     // <= 2^key_bits
+    const int64_t buckets = kDirClasses * (int64_t)n_pos;           // <= 2^key_bits
     int64_t b = (cap + 255) / 256;
     if (b > (int64_t)sm_count * 8) b = (int64_t)sm_count * 8;
     if (b < 1) b = 1;

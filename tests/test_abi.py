@@ -136,7 +136,7 @@ def test_tuning_knobs_validate_and_round_trip_without_gpu():
         assert lib.splat_set_tuning(L.TUNE_BRUTE_TILE, 48) == L.ERR_INVALID
         assert lib.splat_set_tuning(L.TUNE_BRUTE_TILE, 128) == L.OK
         assert lib.splat_set_tuning(L.TUNE_RAY_ORDER, 3) == L.ERR_INVALID
-        assert lib.splat_set_tuning(L.TUNE_RAY_ORDER, 21) == L.ERR_INVALID
+        assert lib.splat_set_tuning(L.TUNE_RAY_ORDER, 23) == L.ERR_INVALID
         assert lib.splat_set_tuning(L.TUNE_RAY_ORDER, 20) == L.OK
         assert lib.splat_get_tuning(L.TUNE_TEST_WAIT_STALL) == 0  # off by default
         assert lib.splat_set_tuning(L.TUNE_TEST_WAIT_STALL, -1) == L.ERR_INVALID
