@@ -167,21 +167,6 @@ __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
         unsigned long long& s_dbase = s_dbase2[par];
         unsigned long long& s_sbase = s_sbase2[par];
         const int64_t k = base + threadIdx.x;
-#ifdef SPLAT_EVOLVE_PREFETCH
-        {
-            // the next iteration's ray planes into L2 while this one computes
-            // (1-D bulk prefetch, a hint with no completion; whole tiles only)
-            const int64_t nb = base + (int64_t)gridDim.x * kEvolveThreads;
-            if (wid == 0 && nb + kEvolveThreads <= n && lane < kPlanes + 3) {
-                const void* src = lane < kPlanes ? (const void*)(A.in.f + (int64_t)lane * A.in.cap + nb)
-                                : lane == kPlanes ? (const void*)(A.in.ignore + nb)
-                                : lane == kPlanes + 1 ? (const void*)(A.in.id + nb) : (const void*)(A.hit_idx + nb);
-                if ((reinterpret_cast<uintptr_t>(src) & 15u) == 0u)  // 16-byte aligned starts only
-                    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(kEvolveThreads * 4)
-                                 : "memory");
-            }
-        }
-#endif
         bool keep = false, dif = false, sky = false;
         RayState r, o;
         uint32_t id = 0;

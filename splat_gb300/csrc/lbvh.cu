@@ -557,21 +557,13 @@ cudaError_t launch_lbvh_build(const splat_ftri_t* ftri, int64_t n_tris, int leaf
 // The order inside a bucket is the atomics' order: only which rays share a
 // warp changes with it, never a result.
 constexpr int kOrderMaxBits = 22;
-#ifdef SPLAT_ORDER_MAJOR
-constexpr int kDirClasses = 24, kDirBits = 5;  // octant x the largest |component|'s axis
-#else
-constexpr int kDirClasses = 8, kDirBits = 3;   // octant
-#endif
+constexpr int kDirClasses = 8, kDirBits = 3;  // direction octants
 
 __device__ __forceinline__ uint32_t ray_key(const float* __restrict__ f, int64_t cap, const int32_t* __restrict__ ignore,
                                             const int32_t* __restrict__ bvh_pos, int64_t n_tris, int pos_shift,
                                             uint32_t n_pos, int64_t k) {
-    const float dx = f[3 * cap + k], dy = f[4 * cap + k], dz = f[5 * cap + k];
-    uint32_t cls = (dx < 0.0f ? 1u : 0u) | (dy < 0.0f ? 2u : 0u) | (dz < 0.0f ? 4u : 0u);
-    if (kDirClasses == 24) {
-        const float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
-        cls = cls * 3u + (ax >= ay && ax >= az ? 0u : (ay >= az ? 1u : 2u));
-    }
+    const uint32_t cls = (f[3 * cap + k] < 0.0f ? 1u : 0u) | (f[4 * cap + k] < 0.0f ? 2u : 0u) |
+                         (f[5 * cap + k] < 0.0f ? 4u : 0u);
     const int32_t ig = ignore[k];
     const uint32_t pos = (ig >= 1 && (int64_t)ig <= n_tris) ? (uint32_t)bvh_pos[ig] : 0u;
     return cls * n_pos + (pos >> pos_shift);
