@@ -138,6 +138,10 @@ def test_tuning_knobs_validate_and_round_trip_without_gpu():
         assert lib.splat_set_tuning(L.TUNE_RAY_ORDER, 3) == L.ERR_INVALID
         assert lib.splat_set_tuning(L.TUNE_RAY_ORDER, 23) == L.ERR_INVALID
         assert lib.splat_set_tuning(L.TUNE_RAY_ORDER, 20) == L.OK
+        assert lib.splat_get_tuning(L.TUNE_COUNT_WORK) == 0 and lib.splat_get_tuning(L.TUNE_BATCH_PERSISTENT) == 0
+        assert lib.splat_set_tuning(L.TUNE_COUNT_WORK, 2) == L.ERR_INVALID
+        assert lib.splat_set_tuning(L.TUNE_BATCH_PERSISTENT, 9) == L.ERR_INVALID
+        assert lib.splat_hit_work(None, 0, None) == L.ERR_INVALID
         assert lib.splat_get_tuning(L.TUNE_TEST_WAIT_STALL) == 0  # off by default
         assert lib.splat_set_tuning(L.TUNE_TEST_WAIT_STALL, -1) == L.ERR_INVALID
         assert lib.splat_set_tuning(L.TUNE_TEST_WAIT_STALL, 0) == L.OK

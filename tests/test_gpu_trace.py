@@ -309,3 +309,34 @@ def test_ray_ranges_on_concurrent_streams(torch_cuda, accum):
     finally:
         L.check(lib.splat_set_tuning(L.TUNE_TRACE_SPLIT, old))
     assert one.sum() > 0
+
+
+def test_counted_traversal_work_matches_the_frame(torch_cuda):
+    """The counting kernels (SPLAT_TUNE_COUNT_WORK) trace the same rays as
+    the plain ones -- same map, same statistics -- and count every traced
+    ray once per bounce; splat_hit_work reads and clears the counters."""
+    import ctypes as C
+
+    from splat_gb300 import _lib as L
+    from splat_gb300 import tracer
+
+    lib = L.load()
+    wl = S.menger(light=S.scaled_light(S.menger().light, 256))
+    scene = tracer.Scene(wl.tris, wl.first_diffuse, bvh=True)
+    ref, sref = _gpu(wl, scene=scene)
+    work = (C.c_int64 * 4)()
+    stream = torch_cuda.cuda.current_stream().cuda_stream
+    L.check(lib.splat_hit_work(work, 1, stream))
+    old = lib.splat_get_tuning(L.TUNE_COUNT_WORK)
+    try:
+        L.check(lib.splat_set_tuning(L.TUNE_COUNT_WORK, 1))
+        got, sg = _gpu(wl, scene=scene)
+    finally:
+        L.check(lib.splat_set_tuning(L.TUNE_COUNT_WORK, old))
+    L.check(lib.splat_hit_work(work, 1, stream))
+    nodes, pre, full, rays = (int(work[i]) for i in range(4))
+    assert np.array_equal(got, ref) and sg == sref
+    assert rays == sum(sref["rays_per_bounce"])
+    assert nodes > rays and pre >= full > 0
+    L.check(lib.splat_hit_work(work, 0, stream))
+    assert all(int(work[i]) == 0 for i in range(4))  # cleared by the previous read
