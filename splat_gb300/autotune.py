@@ -51,6 +51,7 @@ KNOB_CHOICES = {
 
 # knobs that the batch engine's kernels read
 BATCH_KNOB_CHOICES = {
+    L.TUNE_BVH_PACKET: (0, 1, 2, 3, 4, 5),
     L.TUNE_BVH_BLOCKS_PER_SM: (8, 16, 32),
     L.TUNE_EVOLVE_BLOCKS_PER_SM: (4, 8, 16),
     L.TUNE_SPLAT_BLOCKS_PER_SM: (4, 8, 16),

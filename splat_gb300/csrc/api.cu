@@ -111,16 +111,7 @@ Work carve_work(void* ws, int64_t cap) {
 // Traversal form of bounce b (1-based) under the SPLAT_TUNE_BVH_PACKET knob:
 // 0 one ray per lane; 1 warp packets; 2, 3 per-warp choice by ray spread
 // (loose, tight thresholds).
-int32_t packet_for(int32_t b) {
-    switch (g_tune[SPLAT_TUNE_BVH_PACKET]) {
-        case 1: return b == 1 ? 1 : 0;
-        case 2: return 1;
-        case 3: return b == 1 ? 1 : 2;
-        case 4: return b == 1 ? 1 : 3;
-        case 5: return 2;
-        default: return 0;
-    }
-}
+int32_t packet_for(int32_t b) { return packet_form(g_tune[SPLAT_TUNE_BVH_PACKET], b == 1); }
 
 bool valid_material(const splat_material_t* m) {
     return m && m->kind >= SPLAT_MATERIAL_LINEAR_REF && m->kind <= SPLAT_MATERIAL_SELLMEIER;
@@ -1330,6 +1321,7 @@ cudaError_t batch_enqueue_pass(splat_batch* b, cudaStream_t st, int32_t last, in
     a.bar = reinterpret_cast<unsigned*>(&b->counts[kPassBar]);
     a.hit_idx = b->hit;
     a.err = b->d_err;
+    a.packet_mode = g_tune[SPLAT_TUNE_BVH_PACKET];
     {
         ProfScope ps(SPLAT_KERNEL_BATCH, st);
         e = launch_batch_pass(a, share, sm_count_current(), st);

@@ -9,7 +9,8 @@
 //             each item starting this tick its offset in the ray pool, after
 //             the survivors of the previous tick
 //   generate  rays_from_light of those items (src/ray_generators.jl:64-97)
-//   hit       per ray, its item's four-wide BVH or a per-ray brute loop
+//   hit       its item's four-wide BVH (a warp of one item's coherent rays
+//             as a packet) or a per-ray brute loop
 //   evolve    per ray, evolve_ray with its item's material, seed and bounce
 //             (src/tracer.jl:181-201); compaction and the diffuse-ray queue
 //             as in the single-scene step
@@ -145,34 +146,58 @@ __global__ void batch_generate_kernel(const BatchItem* __restrict__ items, const
     generate_phase(items, fresh, out, blockIdx.x, gridDim.x);
 }
 
+// A warp whose 32 rays all belong to one BVH item may walk them as a packet
+// (bvh4_closest_packet on pstack, the warp's kPacketStack entries of shared
+// memory), by packet_form of packet_mode and of whether the item is on its
+// first bounce this tick; every other warp traces one ray per lane.
 template <bool ANY_BRUTE>
 __device__ __forceinline__ void hit_phase(RaySoA in, const int64_t* __restrict__ count,
                                           const BatchItem* __restrict__ items, int32_t* hit_idx, int32_t* err,
-                                          unsigned long long* fetch) {
+                                          unsigned long long* fetch, int tick, int packet_mode, int2* pstack) {
     const int64_t n = *count;
+    const int lane = threadIdx.x & 31;
     int2 stack[kBvhStack];
     RaySrc src{};
     src.f = in.f;
     src.ignore = in.ignore;
     src.cap = in.cap;
-    for_each_ray(n, fetch, [&](int64_t k) {
+    for_each_warp_batch(n, fetch, [&](int64_t base) {
+        const bool valid = base + lane < n;
+        const int64_t k = valid ? base + lane : base;  // idle lanes repeat lane 0's ray
         const HitRay r = load_hit_ray<false>(src, k);
-        const BatchItem& it = items[in.id[k] >> kSlotShift];
+        const uint32_t slot = in.id[k] >> kSlotShift;
+        const BatchItem& it = items[slot];
+        const bool bvh = !ANY_BRUTE || (it.hitter == SPLAT_HITTER_BVH && it.nodes4);
+        const uint32_t slot0 = __shfl_sync(0xffffffffu, slot, 0);
+        bool packet = false;
+        if (packet_mode > 0 && __all_sync(0xffffffffu, bvh & (slot == slot0))) {
+            const int form = packet_form(packet_mode, tick == it.start_tick);  // warp-uniform: one item
+            packet = form == 1 || (form >= 2 && packet_coherent(r, form, bvh4_extent(it.nodes4)));
+        }
         float best;
         int32_t bi;
-        if (!ANY_BRUTE || (it.hitter == SPLAT_HITTER_BVH && it.nodes4))
-            bvh4_closest(r, Bvh4View{it.nodes4, it.bvh_tris}, stack, err, best, bi);
-        else
-            brute_closest(r, it.brute, it.brute_boxes, it.n_recs, best, bi);
-        hit_idx[k] = bi;
+        if (packet) {
+            bvh4_closest_packet(r, valid, Bvh4View{it.nodes4, it.bvh_tris}, pstack, err, best, bi);
+        } else if (valid) {
+            if (bvh)
+                bvh4_closest(r, Bvh4View{it.nodes4, it.bvh_tris}, stack, err, best, bi);
+            else
+                brute_closest(r, it.brute, it.brute_boxes, it.n_recs, best, bi);
+        }
+        if (valid) hit_idx[k] = bi;
     });
 }
 
+constexpr int kBatchHitThreads = 128;
+
 template <bool ANY_BRUTE>
-__global__ void __launch_bounds__(128) batch_hit_kernel(RaySoA in, const int64_t* __restrict__ count,
-                                                        const BatchItem* __restrict__ items, int32_t* hit_idx,
-                                                        int32_t* err, unsigned long long* fetch) {
-    hit_phase<ANY_BRUTE>(in, count, items, hit_idx, err, fetch);
+__global__ void __launch_bounds__(kBatchHitThreads) batch_hit_kernel(RaySoA in, const int64_t* __restrict__ count,
+                                                                     const BatchItem* __restrict__ items,
+                                                                     int32_t* hit_idx, int32_t* err,
+                                                                     unsigned long long* fetch, int tick,
+                                                                     int packet_mode) {
+    __shared__ int2 s_pstack[kBatchHitThreads / 32][kPacketStack];
+    hit_phase<ANY_BRUTE>(in, count, items, hit_idx, err, fetch, tick, packet_mode, s_pstack[threadIdx.x >> 5]);
 }
 
 constexpr int kBatchThreads = 256;
@@ -359,6 +384,7 @@ template <int MK>
 __global__ void __launch_bounds__(kBatchThreads, 2) batch_pass_kernel(BatchPassArgs P) {
     const BatchItem* items = reinterpret_cast<const BatchItem*>(P.items);
     FreshList* fresh = reinterpret_cast<FreshList*>(P.fresh);
+    __shared__ int2 s_pstack[kBatchThreads / 32][kPacketStack];
     const unsigned nblk = gridDim.x;
     unsigned waits = 0;
     for (int i = 0; i < P.n_ticks; ++i) {
@@ -371,7 +397,8 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_pass_kernel(BatchPassA
         if (!grid_wait(P.bar, ++waits * nblk, P.err)) return;
         generate_phase(items, fresh, cur, blockIdx.x, nblk);
         if (!grid_wait(P.bar, ++waits * nblk, P.err)) return;
-        hit_phase<true>(cur, &P.count[i], items, P.hit_idx, P.err, &P.fetch[i]);
+        hit_phase<true>(cur, &P.count[i], items, P.hit_idx, P.err, &P.fetch[i], tick, P.packet_mode,
+                        s_pstack[threadIdx.x >> 5]);
         if (i > 0) {
             const int64_t q0 = P.qmark[i - 1], q1 = P.qmark[i];
             for_each_ray(q1 - q0, &P.splat_fetch[i - 1], [&](int64_t k) { splat_one(P.queue, q0 + k, items); });
@@ -441,14 +468,17 @@ cudaError_t launch_batch_trace(const BatchTickArgs& a, cudaStream_t s) {
         ++g_launches;
     }
     if (a.cap_rays > 0) {
+        const int mode = g_tune[SPLAT_TUNE_BVH_PACKET];
         if (a.any_brute)
             batch_hit_kernel<true><<<resident_grid(reinterpret_cast<const void*>(batch_hit_kernel<true>), a.cap_rays,
-                                                   a.sm_count, 128, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]),
-                                     128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch);
+                                                   a.sm_count, kBatchHitThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]),
+                                     kBatchHitThreads, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch,
+                                                               a.tick, mode);
         else
             batch_hit_kernel<false><<<resident_grid(reinterpret_cast<const void*>(batch_hit_kernel<false>), a.cap_rays,
-                                                    a.sm_count, 128, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]),
-                                      128, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch);
+                                                    a.sm_count, kBatchHitThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]),
+                                      kBatchHitThreads, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch,
+                                                                a.tick, mode);
         ++g_launches;
         const int eg = grid_cap(a.cap_rays, kBatchThreads, a.sm_count, g_tune[SPLAT_TUNE_EVOLVE_BLOCKS_PER_SM]);
 #define SPLAT_BATCH_EVOLVE(MK)                                                                            \

@@ -657,55 +657,22 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_refill_kernel(RaySrc src
         });
 }
 
-// Spread of a warp's rays, max over axes of (max - min) of a coordinate.
-__device__ __forceinline__ float warp_spread(float a, float b, float c) {
-    float m = 0.0f;
-    const float v[3] = {a, b, c};
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        float lo = v[i], hi = v[i];
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
-            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
-        }
-        m = fmaxf(m, hi - lo);
-    }
-    return m;
-}
-
 // Packet form: each warp traverses its 32 rays together (bvh4_closest_packet)
 // on a shared-memory stack.  ADAPT: per warp, packets only when its rays are
-// nearly parallel (direction spread <= dir_spread) and close together (origin
-// spread <= org_spread x the scene's extent); otherwise one ray per lane.
+// coherent by packet_coherent's thresholds of `form` (2 loose, 3 tight);
+// otherwise one ray per lane.
 template <bool AOS, bool ADAPT, bool COUNT = false>
 __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_packet_kernel(RaySrc src, Bvh4View bvh,
                                                                       int32_t* __restrict__ hit_idx,
                                                                       float* __restrict__ hit_t, int32_t* err,
-                                                                      float dir_spread, float org_spread) {
+                                                                      int form) {
     WorkCount wc{0u, 0u, 0u};
     uint32_t rays = 0;
-    __shared__ int s_stack[kBvhThreads / 32][kPacketStack];
-    int* stack = s_stack[threadIdx.x >> 5];
+    __shared__ int2 s_stack[kBvhThreads / 32][kPacketStack];
+    int2* stack = s_stack[threadIdx.x >> 5];
     const int64_t n = src.d_count ? *src.d_count : src.n;
     const int lane = threadIdx.x & 31;
-    float extent = 0.0f;
-    if (ADAPT) {
-        const Bvh4Node& root = bvh.nodes[0];
-        const float4 lx = __ldg(&root.lox), hx = __ldg(&root.hix), ly = __ldg(&root.loy), hy = __ldg(&root.hiy);
-        const float4 lz = __ldg(&root.loz), hz = __ldg(&root.hiz);
-        const int nc = __ldg(&root.meta.x);
-        float lo[3] = {lx.x, ly.x, lz.x}, hi[3] = {hx.x, hy.x, hz.x};
-        for (int i = 1; i < nc; ++i) {
-            lo[0] = fminf(lo[0], comp(lx, i));
-            lo[1] = fminf(lo[1], comp(ly, i));
-            lo[2] = fminf(lo[2], comp(lz, i));
-            hi[0] = fmaxf(hi[0], comp(hx, i));
-            hi[1] = fmaxf(hi[1], comp(hy, i));
-            hi[2] = fmaxf(hi[2], comp(hz, i));
-        }
-        extent = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
-    }
+    const float extent = ADAPT ? bvh4_extent(bvh.nodes) : 0.0f;
     int2 lane_stack[ADAPT ? kBvhStack : 1];
     for_each_warp_batch(n, src.fetch, [&](int64_t base) {
         const bool valid = base + lane < n;
@@ -714,11 +681,7 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_packet_kernel(RaySrc src
         const HitRay r = load_hit_ray<AOS>(src, k);
         float best;
         int32_t bi;
-        bool packet = true;
-        if (ADAPT) {
-            const float ds = warp_spread(r.dx, r.dy, r.dz), os = warp_spread(r.ox, r.oy, r.oz);
-            packet = ds <= dir_spread && os <= org_spread * extent;
-        }
+        const bool packet = !ADAPT || packet_coherent(r, form, extent);
         if (packet) {
             bvh4_closest_packet(r, valid, bvh, stack, err, best, bi, COUNT ? &wc : nullptr);
         } else if (ADAPT && valid) {
@@ -748,24 +711,24 @@ static void launch_bvh4_form(const RaySrc& rays, int64_t cap, const Bvh4View& bv
         return rays.fetch ? resident_grid(k, cap, sm_count, kBvhThreads, knob) : grid_for(cap, kBvhThreads, sm_count, knob);
     };
     if (rays.packet) {
-        // packet = 1: every warp; 2, 3: per warp by ray spread (loose, tight)
-        const float ds = rays.packet == 2 ? 0.3f : 0.1f, os = rays.packet == 2 ? 0.05f : 0.01f;
-        if (rays.packet == 1) {
+        // packet_form: 1 every warp; 2, 3 per warp by ray spread (loose, tight)
+        const int form = rays.packet;
+        if (form == 1) {
             const int grid = grid_of(reinterpret_cast<const void*>(hit_bvh4_packet_kernel<false, false, COUNT>));
             if (rays.aos)
                 hit_bvh4_packet_kernel<true, false, COUNT><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err,
-                                                                                       ds, os);
+                                                                                       form);
             else
                 hit_bvh4_packet_kernel<false, false, COUNT><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t,
-                                                                                        err, ds, os);
+                                                                                        err, form);
         } else {
             const int grid = grid_of(reinterpret_cast<const void*>(hit_bvh4_packet_kernel<false, true, COUNT>));
             if (rays.aos)
                 hit_bvh4_packet_kernel<true, true, COUNT><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err,
-                                                                                      ds, os);
+                                                                                      form);
             else
                 hit_bvh4_packet_kernel<false, true, COUNT><<<grid, kBvhThreads, 0, s>>>(rays, bvh, hit_idx, hit_t, err,
-                                                                                       ds, os);
+                                                                                       form);
         }
         return;
     }

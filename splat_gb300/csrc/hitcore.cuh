@@ -124,8 +124,8 @@ __device__ __forceinline__ float min3f(float a, float b, float c) {
 // node's per-axis float4s, so the test needs no per-axis min / max: each
 // distance is the one min(a, b) / max(a, b) of the two planes would pick,
 // bit for bit (lo <= hi for every real child; the empty slots, lo = +inf and
-// hi = -inf, come out with t0 > tmax, and the child count rejects them
-// anyway).  t0 is the entry distance clamped at the origin, max(tmin, 0):
+// hi = -inf, come out with t0 = +inf > tmax = -inf whatever the ray, as the
+// inverse direction is finite and non-zero, and are never entered).  t0 is the entry distance clamped at the origin, max(tmin, 0):
 // for non-NaN values (tmin <= tmax and tmax >= 0) is t0 <= tmax, and, as
 // every accepted hit has t > 0, tmin <= best is t0 <= best, so a child is
 // entered exactly when the unclamped test enters it.
@@ -175,12 +175,11 @@ __device__ __forceinline__ void bvh4_closest(const HitRay& r, const Bvh4View& bv
             const Bvh4Node* nd = bvh.nodes + ref;
             if (wc) ++wc->nodes;
             const int4 c = __ldg(&nd->c);
-            const int nc = __ldg(&nd->meta.x);
             float tmin[4], tmax[4], key[4];
             node4_slabs(nd, ix, iy, iz, oix, oiy, oiz, tmin, tmax);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const bool h = (i < nc) & (tmin[i] <= tmax[i]) & (tmin[i] <= best);  // tmin: clamped at 0
+                const bool h = (tmin[i] <= tmax[i]) & (tmin[i] <= best);  // tmin: clamped at 0; empty slots fail
                 key[i] = h ? fminf(tmin[i], kMax) : kInf;
             }
             float k0 = key[0], k1 = key[1], k2 = key[2], k3 = key[3];
@@ -299,12 +298,11 @@ __device__ __forceinline__ void bvh4_refill_loop(int64_t n, unsigned long long* 
         } else if (node >= 0) {
             const Bvh4Node* nd = bvh.nodes + node;
             const int4 c = __ldg(&nd->c);
-            const int nc = __ldg(&nd->meta.x);
             float tmin[4], tmax[4], key[4];
             node4_slabs(nd, ix, iy, iz, oix, oiy, oiz, tmin, tmax);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const bool h = (i < nc) & (tmin[i] <= tmax[i]) & (tmin[i] <= best);  // tmin: clamped at 0
+                const bool h = (tmin[i] <= tmax[i]) & (tmin[i] <= best);  // tmin: clamped at 0; empty slots fail
                 key[i] = h ? fminf(tmin[i], kMax) : kInf;
             }
             float k0 = key[0], k1 = key[1], k2 = key[2], k3 = key[3];
@@ -368,17 +366,23 @@ __device__ __forceinline__ void bvh4_refill_loop(int64_t n, unsigned long long* 
 // hit, so the result equals the per-ray traversal and brute force.  For
 // coherent rays (a light's primary rays, refraction through smooth glass)
 // the union of the lanes' paths is little more than one ray's path, and the
-// warp runs it with all lanes busy.  stack: kPacketStack ints shared by the
-// warp; every lane writes every entry (same value), so no warp barrier.
+// warp runs it with all lanes busy.  A pushed child keeps the warp's
+// smallest entry distance; it is popped only while that distance is at or
+// before the largest best hit of the warp's lanes (the per-ray form's pop
+// test, taken over the warp: a lane entered the child at or after that
+// distance, and a lane whose best hit is nearer cannot need it).  stack:
+// kPacketStack (ref, entry distance bits) pairs shared by the warp; every
+// lane writes every entry (same value), so no warp barrier.
 constexpr int kPacketStack = 128;
 
-__device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid, const Bvh4View& bvh, int* stack,
+__device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid, const Bvh4View& bvh, int2* stack,
                                                     int32_t* err, float& best_out, int32_t& bi_out,
                                                     WorkCount* wc = nullptr) {
     const float kInf = __int_as_float(0x7f800000);
     const float ix = safe_inv(r.dx), iy = safe_inv(r.dy), iz = safe_inv(r.dz);
     const float oix = r.ox * ix, oiy = r.oy * iy, oiz = r.oz * iz;
     float best = kInf;
+    float reach = kInf;  // the largest best hit over the warp's valid lanes
     int32_t bi = 1;
     int sp = 0;
     int ref = 0;
@@ -387,7 +391,6 @@ __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid,
             const Bvh4Node* nd = bvh.nodes + ref;
             if (wc && valid) ++wc->nodes;
             const int4 c = __ldg(&nd->c);
-            const int nc = __ldg(&nd->meta.x);
             float tmin[4], tmax[4];
             node4_slabs(nd, ix, iy, iz, oix, oiy, oiz, tmin, tmax);
             unsigned u[4];
@@ -397,7 +400,7 @@ __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid,
                 // their bits, so its bits are the sort key (a -0 from the max sorts
                 // last: order only, never which children are entered)
                 const float t0 = tmin[i];
-                const bool h = valid & (i < nc) & (t0 <= tmax[i]) & (t0 <= best);
+                const bool h = valid & (t0 <= tmax[i]) & (t0 <= best);  // empty slots fail
                 u[i] = __reduce_min_sync(0xffffffffu, h ? __float_as_uint(t0) : 0xffffffffu);
             }
             unsigned k0 = u[0], k1 = u[1], k2 = u[2], k3 = u[3];
@@ -419,9 +422,9 @@ __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid,
 #undef SPLAT_USWAP
             if (k0 != 0xffffffffu) {
                 if (sp + 3 <= kPacketStack) {
-                    if (k3 != 0xffffffffu) stack[sp++] = r3;
-                    if (k2 != 0xffffffffu) stack[sp++] = r2;
-                    if (k1 != 0xffffffffu) stack[sp++] = r1;
+                    if (k3 != 0xffffffffu) stack[sp++] = make_int2(r3, (int)k3);
+                    if (k2 != 0xffffffffu) stack[sp++] = make_int2(r2, (int)k2);
+                    if (k1 != 0xffffffffu) stack[sp++] = make_int2(r1, (int)k1);
                 } else if (threadIdx.x % 32 == 0) {
                     atomicOr(err, 2);
                 }
@@ -448,12 +451,66 @@ __device__ __forceinline__ void bvh4_closest_packet(const HitRay& r, bool valid,
                     bi = idx;
                 }
             }
+            // best >= 0 (or +inf), so its bits order as the floats
+            reach = __uint_as_float(__reduce_max_sync(0xffffffffu, valid ? __float_as_uint(best) : 0u));
         }
-        if (sp == 0) break;
-        ref = stack[--sp];
+        bool found = false;
+        while (sp > 0) {
+            const int2 e = stack[--sp];
+            if (__int_as_float(e.y) <= reach) {  // a -0 entry compares as 0
+                ref = e.x;
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
     }
     best_out = best;
     bi_out = bi;
+}
+
+// Spread of a warp's rays, max over axes of (max - min) of a coordinate.
+__device__ __forceinline__ float warp_spread(float a, float b, float c) {
+    float m = 0.0f;
+    const float v[3] = {a, b, c};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float lo = v[i], hi = v[i];
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+            lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+            hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        }
+        m = fmaxf(m, hi - lo);
+    }
+    return m;
+}
+
+// Largest extent of the scene: the root's child boxes, max over axes.
+__device__ __forceinline__ float bvh4_extent(const Bvh4Node* nodes) {
+    const Bvh4Node& root = nodes[0];
+    const float4 lx = __ldg(&root.lox), hx = __ldg(&root.hix), ly = __ldg(&root.loy), hy = __ldg(&root.hiy);
+    const float4 lz = __ldg(&root.loz), hz = __ldg(&root.hiz);
+    const int nc = __ldg(&root.meta.x);
+    float lo[3] = {lx.x, ly.x, lz.x}, hi[3] = {hx.x, hy.x, hz.x};
+    for (int i = 1; i < nc; ++i) {
+        lo[0] = fminf(lo[0], comp(lx, i));
+        lo[1] = fminf(lo[1], comp(ly, i));
+        lo[2] = fminf(lo[2], comp(lz, i));
+        hi[0] = fmaxf(hi[0], comp(hx, i));
+        hi[1] = fmaxf(hi[1], comp(hy, i));
+        hi[2] = fmaxf(hi[2], comp(hz, i));
+    }
+    return fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+}
+
+// Packet forms 2 / 3: the warp's rays are nearly parallel (direction spread
+// <= 0.3 / 0.1) and close together (origin spread <= 0.05 / 0.01 x the
+// scene's extent).  All 32 lanes call.
+__device__ __forceinline__ bool packet_coherent(const HitRay& r, int form, float extent) {
+    const float dir_spread = form == 2 ? 0.3f : 0.1f, org_spread = form == 2 ? 0.05f : 0.01f;
+    const float ds = warp_spread(r.dx, r.dy, r.dz), os = warp_spread(r.ox, r.oy, r.oz);
+    return ds <= dir_spread && os <= org_spread * extent;
 }
 
 // Closest hit of one ray over hit records in reference-index order (the

@@ -26,10 +26,25 @@ struct RaySrc {
     const int64_t* d_count;    // active count on the device (SoA)
     int64_t n;                 // ray count when d_count is null
     unsigned long long* fetch; // zeroed work counter: warps take rays 32 at a time (nullptr: grid-stride)
-    int32_t packet;            // four-wide BVH: warp packet traversal (1) or one ray per lane (0)
+    int32_t packet;            // four-wide BVH: packet_form of the launch (0 one ray per lane)
     const int32_t* perm;       // BVH hitters: the k-th ray traced is ray perm[k] (nullptr: ray k); results
                                // go to the ray's own index
 };
+
+// Which traversal a warp of four-wide BVH rays takes, from
+// SPLAT_TUNE_BVH_PACKET and whether the rays are on their first bounce:
+// 0 one ray per lane, 1 a packet, 2 / 3 a packet when the warp's rays are
+// coherent by the loose / tight thresholds of packet_coherent (hitcore.cuh).
+__host__ __device__ inline int packet_form(int mode, bool first_bounce) {
+    switch (mode) {
+        case 1: return first_bounce ? 1 : 0;
+        case 2: return 1;
+        case 3: return first_bounce ? 1 : 2;
+        case 4: return first_bounce ? 1 : 3;
+        case 5: return 2;
+        default: return 0;
+    }
+}
 
 // Flattened BVH2 node (Aila & Laine 2009 layout): the boxes of both children
 // and their references.  ref >= 0: inner node index; ref < 0: leaf,
@@ -43,7 +58,8 @@ struct __align__(16) BvhNode {
 static_assert(sizeof(BvhNode) == 64, "BvhNode layout");
 
 // Four-wide node collapsed from the binary tree: child i's box in
-// component i of the six float4s; unused slots have count <= i.
+// component i of the six float4s.  Slots i >= meta.x are empty boxes
+// (lo = +inf, hi = -inf), which no ray enters, so traversal needs no count.
 struct __align__(16) Bvh4Node {
     float4 lox, hix, loy, hiy, loz, hiz;
     int4 c;      // child refs (as BvhNode)
@@ -280,6 +296,7 @@ struct BatchPassArgs {
     unsigned* bar;       // grid-wait arrivals
     int32_t* hit_idx;
     int32_t* err;
+    int packet_mode;     // SPLAT_TUNE_BVH_PACKET when the pass was launched
 };
 cudaError_t launch_batch_pass(const BatchPassArgs& a, int share, int sm_count, cudaStream_t s);
 // the two halves of a tick: reserve, generate, hit, evolve; and the splat of the tick's queue

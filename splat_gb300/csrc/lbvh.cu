@@ -410,10 +410,10 @@ __global__ void lbvh_emit_kernel(LbvhView v, const uint32_t* __restrict__ flag4,
                 ref[nc++] = folded(v, g[e]) ? folded_ref(v, g[e]) : (int)idx4[g[e]];
             }
         }
-        for (int s = nc; s < 4; ++s) {
+        for (int s = nc; s < 4; ++s) {  // empty slots: a box no ray enters
             for (int x = 0; x < 3; ++x) {
-                lo[x][s] = lo[x][0];
-                hi[x][s] = hi[x][0];
+                lo[x][s] = __int_as_float(0x7f800000);
+                hi[x][s] = -__int_as_float(0x7f800000);
             }
             ref[s] = ref[0];
         }
@@ -439,13 +439,14 @@ __global__ void lbvh_single_kernel(const float* box, BvhNode* nodes2, Bvh4Node* 
     nd.z = make_float4(b[2], b[5], b[2], b[5]);
     nd.c = make_int4(leaf_ref(0, 1), leaf_ref(0, 1), 0, 0);
     nodes2[0] = nd;
+    const float inf = __int_as_float(0x7f800000);  // slots 2 and 3 empty
     Bvh4Node q;
-    q.lox = make_float4(b[0], b[0], b[0], b[0]);
-    q.hix = make_float4(b[3], b[3], b[3], b[3]);
-    q.loy = make_float4(b[1], b[1], b[1], b[1]);
-    q.hiy = make_float4(b[4], b[4], b[4], b[4]);
-    q.loz = make_float4(b[2], b[2], b[2], b[2]);
-    q.hiz = make_float4(b[5], b[5], b[5], b[5]);
+    q.lox = make_float4(b[0], b[0], inf, inf);
+    q.hix = make_float4(b[3], b[3], -inf, -inf);
+    q.loy = make_float4(b[1], b[1], inf, inf);
+    q.hiy = make_float4(b[4], b[4], -inf, -inf);
+    q.loz = make_float4(b[2], b[2], inf, inf);
+    q.hiz = make_float4(b[5], b[5], -inf, -inf);
     q.c = make_int4(leaf_ref(0, 1), leaf_ref(0, 1), leaf_ref(0, 1), leaf_ref(0, 1));
     q.meta = make_int4(2, 0, 0, 0);
     nodes4[0] = q;

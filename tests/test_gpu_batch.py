@@ -62,16 +62,28 @@ def _check(wl, got, ref, what):
     assert ref.sum() > 0, what
 
 
-def test_batch_equals_single_frames(frames):
+# the batch hit kernel's traversal forms (SPLAT_TUNE_BVH_PACKET): the default
+# (packets on first-bounce warps of one item), none, every warp of one item,
+# and per warp by ray spread
+@pytest.mark.parametrize("packet", [None, 0, 2, 5])
+def test_batch_equals_single_frames(frames, packet):
+    from splat_gb300 import _lib as L
     from splat_gb300 import batch, tracer
 
+    lib = L.load()
     b = batch.Batch(16, 1 << 21)
     texs = []
     for sc, wl in frames:
         tex = tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum)
         b.admit(sc, wl, tex)
         texs.append(tex)
-    done = b.run()
+    old = lib.splat_get_tuning(L.TUNE_BVH_PACKET)
+    try:
+        if packet is not None:
+            L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, packet))
+        done = b.run()
+    finally:
+        L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, old))
     assert sorted(done) == list(range(len(frames)))
     for i, ((sc, wl), tex) in enumerate(zip(frames, texs)):
         _check(wl, tex.cpu().numpy(), _alone(sc, wl), f"frame {i}")
