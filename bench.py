@@ -31,6 +31,10 @@ the rays active in that bounce) per second of device time, whole job.
           separate pass of steps with the splat overlap off, since in the
           timed steps the splat of earlier bounces runs on a side stream
           beside the later bounces.
+* forms:  (menger line, one GPU) the batched form (64 uneven frames, the
+          --workload batched run) and the served form (Poisson 200 req/s,
+          --forms-duration seconds of arrivals over the 32-scene pool), each
+          against the plain per-frame loop, timed in the same run.
 * cpu_baseline: the CPU restatement of the reference (oracle/, OpenMP over
           all host cores) on a bounded sample of the same workload.
 * --impl reference: that CPU implementation timed alone as the reference arm.
@@ -80,6 +84,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the library's default knobs (no autotuning)")
     ap.add_argument("--no-secondary", action="store_true", help="headline workload only")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="menger line: leave out the batched and served forms' figures")
+    ap.add_argument("--forms-duration", type=float, default=15.0,
+                    help="menger line: seconds of Poisson arrivals of its served figure")
     ap.add_argument("--knobs", default=None,
                     help='JSON of knobs by name to set instead of autotuning, e.g. {"ray_order_bits": 20}')
     ap.add_argument("--light-res", type=int, default=0,
@@ -486,12 +494,34 @@ def run_ours(args):
         Kd = min(K, 300)
         out["e2e"]["frames_in_flight"] = {
             str(m): e2e_pipelined(step, wl, Kd, W, stream, world, rank, n_sets=m)["value"] for m in (3, 4)}
+    if args.workload == "menger" and world == 1 and not (args.no_secondary or args.no_forms):
+        # the batched and served forms beside the plain step, device-timed in
+        # this same run; each starts from the library's default knobs and
+        # tunes its own (the plain loops they are compared with run under
+        # both the default and the tuned knobs, the faster kept)
+        tuned_here = A.get_knobs()
+        A.set_knobs(default_knobs)
+        out["forms"] = {"batched": forms_summary(batched_result(args)),
+                        "served": forms_summary(served_result(200.0, args.forms_duration))}
+        A.set_knobs(tuned_here)
     if world == 1 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(wl, args.cpu_seconds)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def forms_summary(res: dict) -> dict:
+    """The keys of a batched / served line that the headline line carries."""
+    keep = ("metric", "value", "unit", "ms_per_step", "config", "plain_per_frame_loop", "speedup_vs_plain_loop",
+            "dropin_per_frame_loop", "speedup_vs_dropin_loop", "maps_identical_to_plain_loop", "pass_forms",
+            "served", "capacity_frames_per_s", "capacity_speedup_vs_plain_loop", "capacity_speedup_vs_dropin_loop")
+    out = {k: res[k] for k in keep if k in res}
+    if "autotune" in res:
+        out["autotune"] = {k: res["autotune"][k] for k in ("crossover_tris", "hitters", "batch_knobs")
+                           if k in res["autotune"]}
+    return out
 
 
 def secondary_device(wl, K, W, stream, flush) -> dict:
@@ -762,6 +792,10 @@ class DropinLoop:
 
 
 def run_batched(args):
+    print(json.dumps(batched_result(args)), flush=True)
+
+
+def batched_result(args) -> dict:
     """64 frames of uneven size: the plain per-frame loop (one
     splat_trace_forward per frame) and the drop-in per-frame loop (the
     reference's trace! forward sequence through the plugin entry points)
@@ -918,11 +952,15 @@ def run_batched(args):
                "maps_identical_to_plain_loop": bool(same_dropin)},
            "speedup_vs_dropin_loop": dropin_ms / batch_ms,
            "primary_rays_per_s": total_rays / (batch_ms / 1e3)}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 # ---------------------------------------------------------------- served
 def run_served(args):
+    print(json.dumps(served_result(args.rate, args.duration)), flush=True)
+
+
+def served_result(rate: float, duration: float) -> dict:
     """Poisson render requests against a 32-scene pool (Menger level 3):
     the continuous-batching server against the plain per-frame loop (FIFO,
     one splat_trace_forward per request), same arrivals; p50 / p99 latency
@@ -947,7 +985,7 @@ def run_served(args):
     for sid in range(32):
         pool.acquire(sid, 0)
         pool.release(sid)
-    arrivals = serve.poisson_arrivals(args.rate, args.duration, seed=6)
+    arrivals = serve.poisson_arrivals(rate, duration, seed=6)
     sids = rng.integers(0, 32, size=len(arrivals))
     reqs = []
     for rid, (t, sid) in enumerate(zip(arrivals, sids)):
@@ -1046,7 +1084,7 @@ def run_served(args):
            "steps": len(reqs), "warmup": 0, "ms_per_step": 1e3 / max(served["frames_per_s"], 1e-9),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic: seeded Poisson arrivals, 32 procedural Menger-3 scenes",
-           "config": {"workload": f"Poisson {args.rate} req/s for {args.duration} s, 32-scene pool (Menger level 3, "
+           "config": {"workload": f"Poisson {rate} req/s for {duration} s, 32-scene pool (Menger level 3, "
                                   f"96,012 tris), per-request rays log-uniform [2^14, 2^22], depth 2-6, 1-16 planes, "
                                   f"maps 256^2-2048^2 int32, light within 5 degrees",
                       "hbm_budget_gb": 150, "scene_loads": pool.loads, "scene_evictions": pool.evictions,
@@ -1059,7 +1097,7 @@ def run_served(args):
            "capacity_speedup_vs_plain_loop": cap_served / cap_plain,
            "capacity_speedup_vs_dropin_loop": cap_served / cap_dropin,
            "speedup_vs_plain_loop": served["frames_per_s"] / max(plain["frames_per_s"], 1e-9)}
-    print(json.dumps(out), flush=True)
+    return out
 
 
 # ---------------------------------------------------------------- render

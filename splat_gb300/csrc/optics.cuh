@@ -225,25 +225,39 @@ __device__ __forceinline__ void handle_optics(const RayState& r, const HitDerivs
     o.dpx = vpar(next_p(r, h, Lc, Xd, Yc));
     o.dpy = vpar(next_p(r, h, Lc, Xc, Yd));
 
-    if (refracts) {
-        o.dir = refract(r.dir, N0, n1c, n2c);
-        D n1d = in_med ? glass(mat, Ld) : air(Ld);
-        D n2d = in_med ? air(Ld) : glass(mat, Ld);
-        if (quirks) {
-            o.ddl = vpar(refract(d_expansion(r, Ld, Xc, Yc), N0, n1d, n2d));
+    // Each direction partial is the refraction or the reflection of the same
+    // dual direction about the same dual normal: both are evaluated once,
+    // before the lanes of a warp part on `refracts`, so a warp whose rays
+    // take both ways runs only the short refract / reflect tails twice.
+    o.dir = refracts ? refract(r.dir, N0, n1c, n2c) : reflect(r.dir, N0);
+    {
+        const auto dv = d_expansion(r, Ld, Xc, Yc);
+        if (refracts && quirks) {
+            const D n1d = in_med ? glass(mat, Ld) : air(Ld);
+            const D n2d = in_med ? air(Ld) : glass(mat, Ld);
+            o.ddl = vpar(refract(dv, N0, n1d, n2d));
         } else {
-            o.ddl = vpar(refract(d_expansion(r, Ld, Xc, Yc), N_at(r, h, T, Ld, Xc, Yc), n1d, n2d));
+            const auto nv = N_at(r, h, T, Ld, Xc, Yc);
+            if (refracts) {
+                const D n1d = in_med ? glass(mat, Ld) : air(Ld);
+                const D n2d = in_med ? air(Ld) : glass(mat, Ld);
+                o.ddl = vpar(refract(dv, nv, n1d, n2d));
+            } else {
+                o.ddl = vpar(reflect(dv, nv));
+            }
         }
-        o.ddx = vpar(refract(d_expansion(r, Lc, Xd, Yc), N_at(r, h, T, Lc, Xd, Yc), n1c, n2c));
-        o.ddy = vpar(refract(d_expansion(r, Lc, Xc, Yq), N_at(r, h, T, Lc, Xc, Yq), n1c, n2c));
-        o.medium = in_med ? 0 : 1;
-    } else {
-        o.dir = reflect(r.dir, N0);
-        o.ddl = vpar(reflect(d_expansion(r, Ld, Xc, Yc), N_at(r, h, T, Ld, Xc, Yc)));
-        o.ddx = vpar(reflect(d_expansion(r, Lc, Xd, Yc), N_at(r, h, T, Lc, Xd, Yc)));
-        o.ddy = vpar(reflect(d_expansion(r, Lc, Xc, Yq), N_at(r, h, T, Lc, Xc, Yq)));
-        o.medium = r.medium;
     }
+    {
+        const auto dv = d_expansion(r, Lc, Xd, Yc);
+        const auto nv = N_at(r, h, T, Lc, Xd, Yc);
+        o.ddx = refracts ? vpar(refract(dv, nv, n1c, n2c)) : vpar(reflect(dv, nv));
+    }
+    {
+        const auto dv = d_expansion(r, Lc, Xc, Yq);
+        const auto nv = N_at(r, h, T, Lc, Xc, Yq);
+        o.ddy = refracts ? vpar(refract(dv, nv, n1c, n2c)) : vpar(reflect(dv, nv));
+    }
+    o.medium = refracts ? (in_med ? 0 : 1) : r.medium;
     o.lam = r.lam;
     o.x = r.x;
     o.y = r.y;
