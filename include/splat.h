@@ -510,7 +510,11 @@ enum {
     SPLAT_TUNE_RAY_ORDER = 10,           /* fused trace step, four-wide BVH: 0 secondary rays traced in compaction
                                             order; 4..22 each bounce after the first groups its rays by (direction
                                             octant, BVH position of the triangle they leave), a key of that many
-                                            bits, before the hit launch (default 0) */
+                                            bits, before the hit launch (default 0).  Batch engine (any value
+                                            above 0): every tick's rays grouped by (item, BVH position of the
+                                            triangle left, octant) before its hit kernel, up to 2^24 buckets
+                                            (positions coarsened by one shift when the items' triangles do not
+                                            fit) */
     SPLAT_TUNE_BRUTE_TILE = 11,          /* brute-force hitter: hit records per stage of its shared-memory ring,
                                             32, 64 (default) or 128 */
     SPLAT_TUNE_COUNT_WORK = 12,          /* four-wide BVH: 0 (default) plain kernels; 1 counting kernels that add

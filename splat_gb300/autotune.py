@@ -10,8 +10,9 @@ timings, and cached in a JSON file (``$SPLAT_TUNE_CACHE`` or
   force, the others by the four-wide BVH (``batch_crossover``,
   ``hitter_for``).  The sweep follows the reference's hitter benchmark
   (rays x triangles, src/scenes/perf_test.jl:9-45);
-* the launch shapes of the batch engine (blocks per SM of its hit, evolve
-  and splat kernels, the splat's texel aggregation), by coordinate descent
+* the launch shapes of the batch engine (its rays' order, the packet form,
+  blocks per SM of its hit, evolve and splat kernels, the splat's texel
+  aggregation), by coordinate descent
   on the time of a captured pass (``tune_batch``); the reference sizes its
   hitter launches with the occupancy API (src/hitters.jl:75,149,214,297,390);
 * the knobs of the plain trace step, including the brute-force tile size,
@@ -51,6 +52,7 @@ KNOB_CHOICES = {
 
 # knobs that the batch engine's kernels read
 BATCH_KNOB_CHOICES = {
+    L.TUNE_RAY_ORDER: (0, 20),
     L.TUNE_BVH_PACKET: (0, 1, 2, 3, 4, 5),
     L.TUNE_BVH_BLOCKS_PER_SM: (8, 16, 32),
     L.TUNE_EVOLVE_BLOCKS_PER_SM: (4, 8, 16),

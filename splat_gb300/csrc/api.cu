@@ -1127,6 +1127,13 @@ struct splat_batch {
     int32_t tick = 0;
     int parity = 0;
     bool dirty = true;
+    // ray order (SPLAT_TUNE_RAY_ORDER > 0): keys, permutation, bucket counts,
+    // scan sums; buckets of the uploaded item table
+    uint32_t* ord_keys = nullptr;
+    int32_t* ord_perm = nullptr;
+    uint32_t* ord_cnt = nullptr;
+    uint32_t* ord_sums = nullptr;
+    int64_t order_buckets = 0;
     cudaGraphExec_t exec = nullptr;
     // captured graphs: the splat of tick t on a side stream beside tick t + 1
     // (queues alternate by tick parity; q2 is allocated at the first such capture)
@@ -1144,9 +1151,16 @@ struct splat_batch {
 
 namespace {
 
+// ray order of the batch: keys and permutation per pool ray, bucket counts
+// and the scan's tile sums for 2^kBatchOrderBits buckets
+size_t batch_order_bytes(int64_t cap) {
+    const int64_t buckets = int64_t(1) << kBatchOrderBits;
+    return 2 * align_up(4 * (size_t)cap) + align_up(4 * (size_t)buckets) + align_up(4 * order_sums_count(buckets));
+}
+
 size_t batch_bytes(int32_t max_items, int64_t cap) {
     return align_up(batch_item_bytes() * (size_t)max_items) + align_up(batch_fresh_bytes()) + 3 * soa_bytes(cap) +
-           align_up(4 * (size_t)cap) + kCounterBytes + kAlign;
+           align_up(4 * (size_t)cap) + kCounterBytes + batch_order_bytes(cap) + kAlign;
 }
 
 void batch_free(splat_batch* b) {
@@ -1179,6 +1193,8 @@ splat_status_t batch_upload(splat_batch* b, cudaStream_t st) {
     const int i = b->stage_idx;
     b->stage_idx ^= 1;
     SPLAT_CUDA(cudaEventSynchronize(b->stage_ev[i]), "batch: stage reuse");
+    b->order_buckets =
+        batch_assign_order_keys(b->h_items.data(), b->used.data(), b->max_items, kBatchOrderBits);
     std::memcpy(b->h_stage[i], b->h_items.data(), b->h_items.size());
     SPLAT_CUDA(cudaMemcpyAsync(b->d_items, b->h_stage[i], b->h_items.size(), cudaMemcpyHostToDevice, st),
                "batch: upload items");
@@ -1267,6 +1283,12 @@ splat_status_t batch_enqueue_tick(splat_batch* b, cudaStream_t st, int32_t* done
         a.any_brute = any_brute;
         a.material_kind = kind < 0 ? -1 : kind;
         a.fetch = reinterpret_cast<unsigned long long*>(&b->counts[3]);
+        const bool order = g_tune[SPLAT_TUNE_RAY_ORDER] > 0 && b->order_buckets > 0;
+        a.order_buckets = order ? b->order_buckets : 0;
+        a.order_keys = b->ord_keys;
+        a.order_cnt = b->ord_cnt;
+        a.order_sums = b->ord_sums;
+        a.order_perm = b->ord_perm;
         if (b->overlap) {
             SPLAT_CUDA(launch_batch_trace(a, st), "batch tick");
             SPLAT_CUDA(cudaEventRecord(b->traced_ev[qp], st), "batch: fork");
@@ -1370,6 +1392,14 @@ splat_status_t splat_batch_create(int32_t max_items, int64_t max_pool_rays, spla
     p += align_up(4 * (size_t)max_pool_rays);
     b->counts = reinterpret_cast<int64_t*>(p);
     b->d_err = reinterpret_cast<int32_t*>(p + 512);
+    p += kCounterBytes;
+    b->ord_keys = reinterpret_cast<uint32_t*>(p);
+    p += align_up(4 * (size_t)max_pool_rays);
+    b->ord_perm = reinterpret_cast<int32_t*>(p);
+    p += align_up(4 * (size_t)max_pool_rays);
+    b->ord_cnt = reinterpret_cast<uint32_t*>(p);
+    p += align_up(4 * (size_t)(int64_t(1) << kBatchOrderBits));
+    b->ord_sums = reinterpret_cast<uint32_t*>(p);
     const size_t table = b->item_bytes * (size_t)max_items;
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
         e = cudaMallocHost(&b->h_stage[i], table);
@@ -1440,8 +1470,7 @@ splat_status_t splat_batch_admit(splat_batch_t* b, const splat_scene_t* scene, c
     g.light_index = 0;
     g.ray_begin = rb;
     BatchSceneRef sc{scene->d_ftri, scene->d_brute, scene->d_boxes, scene->d_nodes4, scene->d_bvh, scene->n_recs,
-                     scene->n_tris,
-                     scene->first_diffuse};
+                     scene->n_tris, scene->first_diffuse, scene->d_bvh_pos};
     const SplatParams sp =
         make_splat(P->spectrum, P->n_lambda, P->upscale, d_map, P->accum, P->frac_bits, P->map_w, P->map_h);
     batch_fill_item(b->h_items.data() + b->item_bytes * (size_t)slot, sc, g, n, P->depth,

@@ -9,6 +9,9 @@
 //             each item starting this tick its offset in the ray pool, after
 //             the survivors of the previous tick
 //   generate  rays_from_light of those items (src/ray_generators.jl:64-97)
+//   order     (optional, SPLAT_TUNE_RAY_ORDER) a counting sort of the rays
+//             by (item, BVH position of the triangle left, direction
+//             octant), so that a warp's rays share an item and a path
 //   hit       its item's four-wide BVH (a warp of one item's coherent rays
 //             as a packet) or a per-ray brute loop
 //   evolve    per ray, evolve_ray with its item's material, seed and bounce
@@ -55,6 +58,10 @@ struct BatchItem {
     int64_t n_rays;
     splat_material_t material;
     SplatParams sp;
+    const int32_t* bvh_pos;  // ray order: BVH position of each reference index
+    int64_t key_base;        // ray order: the item's first bucket position
+    int32_t pos_shift;       // ray order: low position bits dropped
+    int32_t _pad1;
 };
 
 struct FreshList {
@@ -150,10 +157,12 @@ __global__ void batch_generate_kernel(const BatchItem* __restrict__ items, const
 // (bvh4_closest_packet on pstack, the warp's kPacketStack entries of shared
 // memory), by packet_form of packet_mode and of whether the item is on its
 // first bounce this tick; every other warp traces one ray per lane.
+// perm (optional): the rays in ray order, perm[j] the pool index of the j-th.
 template <bool ANY_BRUTE>
 __device__ __forceinline__ void hit_phase(RaySoA in, const int64_t* __restrict__ count,
                                           const BatchItem* __restrict__ items, int32_t* hit_idx, int32_t* err,
-                                          unsigned long long* fetch, int tick, int packet_mode, int2* pstack) {
+                                          unsigned long long* fetch, int tick, int packet_mode, int2* pstack,
+                                          const int32_t* __restrict__ perm = nullptr) {
     const int64_t n = *count;
     const int lane = threadIdx.x & 31;
     int2 stack[kBvhStack];
@@ -163,7 +172,15 @@ __device__ __forceinline__ void hit_phase(RaySoA in, const int64_t* __restrict__
     src.cap = in.cap;
     for_each_warp_batch(n, fetch, [&](int64_t base) {
         const bool valid = base + lane < n;
-        const int64_t k = valid ? base + lane : base;  // idle lanes repeat lane 0's ray
+        const int64_t kk = valid ? base + lane : base;  // idle lanes repeat lane 0's ray
+        int64_t k = kk;
+        if (perm) {
+            k = (int64_t)perm[kk];
+            if ((uint64_t)k >= (uint64_t)n) {  // never: perm is a permutation of 0 .. n - 1
+                atomicOr(err, 4);
+                k = kk;
+            }
+        }
         const HitRay r = load_hit_ray<false>(src, k);
         const uint32_t slot = in.id[k] >> kSlotShift;
         const BatchItem& it = items[slot];
@@ -190,14 +207,48 @@ __device__ __forceinline__ void hit_phase(RaySoA in, const int64_t* __restrict__
 
 constexpr int kBatchHitThreads = 128;
 
-template <bool ANY_BRUTE>
-__global__ void __launch_bounds__(kBatchHitThreads) batch_hit_kernel(RaySoA in, const int64_t* __restrict__ count,
-                                                                     const BatchItem* __restrict__ items,
-                                                                     int32_t* hit_idx, int32_t* err,
-                                                                     unsigned long long* fetch, int tick,
-                                                                     int packet_mode) {
+// ORDER: the rays are read through the ray-order permutation perm (the
+// plain form, without it, keeps its register count and occupancy).
+template <bool ANY_BRUTE, bool ORDER>
+__global__ void __launch_bounds__(kBatchHitThreads, 8) batch_hit_kernel(RaySoA in, const int64_t* __restrict__ count,
+                                                                        const BatchItem* __restrict__ items,
+                                                                        int32_t* hit_idx, int32_t* err,
+                                                                        unsigned long long* fetch, int tick,
+                                                                        int packet_mode,
+                                                                        const int32_t* __restrict__ perm) {
     __shared__ int2 s_pstack[kBatchHitThreads / 32][kPacketStack];
-    hit_phase<ANY_BRUTE>(in, count, items, hit_idx, err, fetch, tick, packet_mode, s_pstack[threadIdx.x >> 5]);
+    hit_phase<ANY_BRUTE>(in, count, items, hit_idx, err, fetch, tick, packet_mode, s_pstack[threadIdx.x >> 5],
+                         ORDER ? perm : nullptr);
+}
+
+// Ray-order keys of the tick's active rays and the size of every bucket
+// (one atomic per group of equal keys in a warp).  A ray's key is its
+// item's base plus the BVH position of the triangle it leaves (0 for a
+// fresh ray), shifted, times 8, plus its direction octant; items without a
+// BVH have one position.
+__global__ void batch_order_count_kernel(RaySoA in, const int64_t* __restrict__ count, int64_t cap_rays,
+                                         const BatchItem* __restrict__ items, uint32_t* __restrict__ keys,
+                                         uint32_t* __restrict__ cnt) {
+    const int64_t n = min(min(in.cap, cap_rays), *count);  // the rays the placement kernel places
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += stride) {
+        const int64_t k = base + lane;
+        const bool valid = k < n;
+        uint32_t key = 0xffffffffu;
+        if (valid) {
+            const BatchItem& it = items[in.id[k] >> kSlotShift];
+            const int32_t ig = in.ignore[k];
+            const uint32_t pos = (it.bvh_pos && ig >= 1 && (int64_t)ig <= it.n_tris)
+                                     ? (uint32_t)it.bvh_pos[ig] >> it.pos_shift : 0u;
+            const uint32_t cls = (in.f[3 * in.cap + k] < 0.0f ? 1u : 0u) | (in.f[4 * in.cap + k] < 0.0f ? 2u : 0u) |
+                                 (in.f[5 * in.cap + k] < 0.0f ? 4u : 0u);
+            key = ((uint32_t)it.key_base + pos) * 8u + cls;
+            keys[k] = key;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        if (valid && lane == __ffs(peers) - 1) atomicAdd(&cnt[key], (uint32_t)__popc(peers));
+    }
 }
 
 constexpr int kBatchThreads = 256;
@@ -469,16 +520,28 @@ cudaError_t launch_batch_trace(const BatchTickArgs& a, cudaStream_t s) {
     }
     if (a.cap_rays > 0) {
         const int mode = g_tune[SPLAT_TUNE_BVH_PACKET];
+        const int32_t* perm = nullptr;
+        if (a.order_buckets > 0 && a.order_perm) {
+            cudaError_t e = cudaMemsetAsync(a.order_cnt, 0, sizeof(uint32_t) * (size_t)a.order_buckets, s);
+            if (e != cudaSuccess) return e;
+            batch_order_count_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(
+                a.cur, a.cur_count, a.cap_rays, items, a.order_keys, a.order_cnt);
+            ++g_launches;
+            e = launch_order_place(a.order_keys, a.cap_rays, a.cur_count, a.order_cnt, a.order_buckets, a.order_sums,
+                                   a.order_perm, a.sm_count, s);
+            if (e != cudaSuccess) return e;
+            perm = a.order_perm;
+        }
+        auto hit = [&](auto kernel) {
+            const int grid = resident_grid(reinterpret_cast<const void*>(kernel), a.cap_rays, a.sm_count,
+                                           kBatchHitThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
+            kernel<<<grid, kBatchHitThreads, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch, a.tick,
+                                                      mode, perm);
+        };
         if (a.any_brute)
-            batch_hit_kernel<true><<<resident_grid(reinterpret_cast<const void*>(batch_hit_kernel<true>), a.cap_rays,
-                                                   a.sm_count, kBatchHitThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]),
-                                     kBatchHitThreads, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch,
-                                                               a.tick, mode);
+            perm ? hit(batch_hit_kernel<true, true>) : hit(batch_hit_kernel<true, false>);
         else
-            batch_hit_kernel<false><<<resident_grid(reinterpret_cast<const void*>(batch_hit_kernel<false>), a.cap_rays,
-                                                    a.sm_count, kBatchHitThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]),
-                                      kBatchHitThreads, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch,
-                                                                a.tick, mode);
+            perm ? hit(batch_hit_kernel<false, true>) : hit(batch_hit_kernel<false, false>);
         ++g_launches;
         const int eg = grid_cap(a.cap_rays, kBatchThreads, a.sm_count, g_tune[SPLAT_TUNE_EVOLVE_BLOCKS_PER_SM]);
 #define SPLAT_BATCH_EVOLVE(MK)                                                                            \
@@ -533,7 +596,28 @@ void batch_fill_item(void* dst, const BatchSceneRef& sc, const GenParams& gen, i
     it.n_rays = n_rays;
     it.material = material;
     it.sp = sp;
+    it.bvh_pos = sc.nodes4 ? sc.bvh_pos : nullptr;
     std::memcpy(dst, &it, sizeof(it));
+}
+
+int64_t batch_assign_order_keys(void* items, const uint8_t* used, int32_t n_slots, int max_bits) {
+    BatchItem* it = reinterpret_cast<BatchItem*>(items);
+    const int64_t limit = (int64_t(1) << max_bits) / 8;  // positions that fit
+    for (int shift = 0; shift < 31; ++shift) {
+        int64_t total = 0;
+        for (int32_t s = 0; s < n_slots; ++s)
+            if (used[s]) total += (it[s].bvh_pos ? (it[s].n_tris >> shift) : 0) + 1;
+        if (total > limit) continue;
+        int64_t base = 0;
+        for (int32_t s = 0; s < n_slots; ++s) {
+            if (!used[s]) continue;
+            it[s].key_base = base;
+            it[s].pos_shift = shift;
+            base += (it[s].bvh_pos ? (it[s].n_tris >> shift) : 0) + 1;
+        }
+        return total * 8;
+    }
+    return 0;
 }
 
 void batch_clear_item(void* dst) {

@@ -129,6 +129,15 @@ cudaError_t launch_ray_order(const float* soa_f, const int32_t* ignore, int64_t 
                              const int32_t* bvh_pos, int64_t n_tris, int key_bits, void* scratch,
                              const int32_t** perm_out, int sm_count, cudaStream_t s);
 
+// The placement half of that counting sort for keys computed elsewhere: cnt
+// holds each bucket's size (buckets entries), is scanned in place into
+// offsets (sums: order_sums_count(buckets) words of scratch), and every one
+// of the d_count rays takes a slot of its bucket in perm (one atomic per
+// group of equal keys in a warp).
+size_t order_sums_count(int64_t buckets);
+cudaError_t launch_order_place(const uint32_t* keys, int64_t cap, const int64_t* d_count, uint32_t* cnt,
+                               int64_t buckets, uint32_t* sums, int32_t* perm, int sm_count, cudaStream_t s);
+
 // scene packing / refit.  scale: device word holding max |vertex coordinate|
 // (float bits), from which every padded box takes pad_abs = 1e-4 max(1, scale).
 // bvh_pos (optional, n_tris + 1 entries): the inverse of bvh_order.
@@ -255,7 +264,13 @@ struct BatchSceneRef {
     const Bvh4Node* nodes4;
     const TriHit* bvh_tris;
     int64_t n_recs, n_tris, first_diffuse;
+    const int32_t* bvh_pos;  // BVH record position of each reference index (nullptr: none)
 };
+
+// Ray order of the batch engine: bucket keys over every item of the table,
+// (item's key base + BVH position of the triangle left >> pos_shift) x 8 +
+// direction octant, at most 2^kBatchOrderBits buckets.
+constexpr int kBatchOrderBits = 24;
 
 struct BatchTickArgs {
     void* items;  // device item table
@@ -274,6 +289,13 @@ struct BatchTickArgs {
     bool any_brute;      // some item in flight uses the brute-force hitter (or has no BVH)
     int material_kind;   // material kind shared by every item in flight, -1 when mixed
     unsigned long long* fetch;  // zeroed work counter of this tick's hit kernel
+    // ray order before the hit kernel (order_buckets > 0): keys and perm of
+    // cap_rays entries, bucket counts (order_buckets) and their scan's sums
+    int64_t order_buckets;
+    uint32_t* order_keys;
+    uint32_t* order_cnt;
+    uint32_t* order_sums;
+    int32_t* order_perm;
 };
 
 cudaError_t launch_batch_tick(const BatchTickArgs& a, cudaStream_t s);
@@ -310,6 +332,11 @@ void batch_fill_item(void* dst, const BatchSceneRef& sc, const GenParams& gen, i
                      int32_t hitter, int32_t start_tick, int32_t quirks, float force_rand,
                      const splat_material_t& material, const SplatParams& sp);
 void batch_clear_item(void* dst);
+// Assigns every used item of a host item table its ray-order key base (items
+// in slot order, each (n_tris >> shift) + 1 positions, one shift for all,
+// the smallest that fits 8 x positions in 2^max_bits buckets); returns the
+// number of buckets.
+int64_t batch_assign_order_keys(void* items, const uint8_t* used, int32_t n_slots, int max_bits);
 void batch_set_seed(void* dst, uint64_t seed);
 
 }  // namespace splat

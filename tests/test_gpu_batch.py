@@ -62,28 +62,43 @@ def _check(wl, got, ref, what):
     assert ref.sum() > 0, what
 
 
+@pytest.fixture()
+def knobs(torch_cuda):
+    """Sets tuning knobs for one test and puts the old values back."""
+    from splat_gb300 import _lib as L
+
+    lib = L.load()
+    saved = {}
+
+    def set_(key, value):
+        if key not in saved:
+            saved[key] = lib.splat_get_tuning(key)
+        L.check(lib.splat_set_tuning(key, value))
+
+    yield set_
+    for key, value in saved.items():
+        L.check(lib.splat_set_tuning(key, value))
+
+
 # the batch hit kernel's traversal forms (SPLAT_TUNE_BVH_PACKET): the default
 # (packets on first-bounce warps of one item), none, every warp of one item,
-# and per warp by ray spread
-@pytest.mark.parametrize("packet", [None, 0, 2, 5])
-def test_batch_equals_single_frames(frames, packet):
+# and per warp by ray spread; with and without the rays of every tick
+# grouped by (item, BVH position of the triangle left, octant) first
+@pytest.mark.parametrize("packet,order", [(None, 0), (0, 0), (2, 0), (5, 0), (0, 20), (2, 20), (5, 20)])
+def test_batch_equals_single_frames(frames, knobs, packet, order):
     from splat_gb300 import _lib as L
     from splat_gb300 import batch, tracer
 
-    lib = L.load()
     b = batch.Batch(16, 1 << 21)
     texs = []
     for sc, wl in frames:
         tex = tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum)
         b.admit(sc, wl, tex)
         texs.append(tex)
-    old = lib.splat_get_tuning(L.TUNE_BVH_PACKET)
-    try:
-        if packet is not None:
-            L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, packet))
-        done = b.run()
-    finally:
-        L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, old))
+    if packet is not None:
+        knobs(L.TUNE_BVH_PACKET, packet)
+    knobs(L.TUNE_RAY_ORDER, order)
+    done = b.run()
     assert sorted(done) == list(range(len(frames)))
     for i, ((sc, wl), tex) in enumerate(zip(frames, texs)):
         _check(wl, tex.cpu().numpy(), _alone(sc, wl), f"frame {i}")
@@ -92,11 +107,17 @@ def test_batch_equals_single_frames(frames, packet):
     assert b.status()["in_flight"] == 0
 
 
-def test_frames_joining_while_others_run(frames):
+@pytest.mark.parametrize("order", [0, 20])
+def test_frames_joining_while_others_run(frames, knobs, order):
     """Continuous batching: frames admitted at different ticks overlap on the
-    device and each still equals its alone result."""
+    device and each still equals its alone result (with the ray order, the
+    items' key ranges are reassigned at every admission while rays are in
+    flight)."""
+    from splat_gb300 import _lib as L
     from splat_gb300 import batch, tracer
 
+    knobs(L.TUNE_RAY_ORDER, order)
+    knobs(L.TUNE_BVH_PACKET, 5 if order else 1)
     b = batch.Batch(8, 1 << 21)
     plan = {0: [3, 0], 1: [2], 2: [1, 5], 4: [4]}
     texs, done = {}, []
@@ -115,9 +136,12 @@ def test_frames_joining_while_others_run(frames):
         _check(wl, tex.cpu().numpy(), _alone(sc, wl), f"frame {i} joined late")
 
 
-def test_graph_capture_and_replay_with_new_seeds(frames):
+@pytest.mark.parametrize("order", [0, 20])
+def test_graph_capture_and_replay_with_new_seeds(frames, knobs, order):
+    from splat_gb300 import _lib as L
     from splat_gb300 import batch, tracer
 
+    knobs(L.TUNE_RAY_ORDER, order)
     b = batch.Batch(8, 1 << 21)
     sel = [0, 2, 3]
     texs = []
