@@ -516,7 +516,8 @@ def forms_summary(res: dict) -> dict:
     """The keys of a batched / served line that the headline line carries."""
     keep = ("metric", "value", "unit", "ms_per_step", "config", "plain_per_frame_loop", "speedup_vs_plain_loop",
             "dropin_per_frame_loop", "speedup_vs_dropin_loop", "maps_identical_to_plain_loop", "pass_forms",
-            "served", "capacity_frames_per_s", "capacity_speedup_vs_plain_loop", "capacity_speedup_vs_dropin_loop")
+            "served", "plain_per_frame_loop_default_knobs", "knobs", "capacity_frames_per_s",
+            "capacity_speedup_vs_plain_loop", "capacity_speedup_vs_dropin_loop")
     out = {k: res[k] for k in keep if k in res}
     if "autotune" in res:
         out["autotune"] = {k: res["autotune"][k] for k in ("crossover_tris", "hitters", "batch_knobs")
@@ -999,8 +1000,23 @@ def served_result(rate: float, duration: float) -> dict:
     # continuous batching; a completed map is delivered (here: dropped, as the
     # plain loop below drops its maps) and the server keeps only maps in flight
     from splat_gb300 import autotune as A
+    from splat_gb300 import batch as B
 
     cross = A.batch_crossover()["crossover_tris"]
+    # the engine's knobs (rays' order, packet form, grid shapes) tuned on a
+    # captured pass of 48 of the stream's requests; the server and the plain
+    # loop then both run under them (the plain loop also under the library
+    # defaults, reported beside)
+    default_knobs = {**A.get_knobs(), **A.get_knobs({L.TUNE_BATCH_PERSISTENT: (0,)})}
+    sample = [wl for _, _, wl in reqs[:48]]
+    s_maps = [tracer.new_light_map(w.map_w, w.map_h, w.n_planes, w.accum) for w in sample]
+    lanes = B.Lanes(2, sample, [pool.resident[sid] for _, sid, _ in reqs[:48]], s_maps, crossover_tris=cross)
+    tuned = A.tune_batch(lanes, [w.seed for w in sample], reps=2, use_cache=False)
+    L.check(lib.splat_set_tuning(L.TUNE_BATCH_PERSISTENT, 0))
+    served_knobs = A.named(A.get_knobs(A.BATCH_KNOB_CHOICES))
+    for e in lanes.engines:
+        e.close()
+    del lanes, s_maps
     srv = serve.Server(pool, budget, max_items=128, on_done=lambda req: None, crossover_tris=cross)
     for t, sid, wl in reqs:
         srv.submit(serve.Request(arrival=t + 0.5, rid=len(srv.pending), scene_id=sid, wl=wl))
@@ -1016,35 +1032,43 @@ def served_result(rate: float, duration: float) -> dict:
     max_rays = max(w.n_rays for _, _, w in reqs)
     ws = torch.empty(int(lib.splat_trace_workspace_size(max_rays)), dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    ev0.record(stream)
-    torch.cuda.synchronize()
-    h0 = time.perf_counter()
-    plain_done = []
-    pending_events = []
-    for t, sid, wl in reqs:
-        arrive = t + 0.5
-        while time.perf_counter() - h0 < arrive:  # a request is served only once it has arrived
-            time.sleep(0.0002)
-        sc = pool.acquire(sid, 0)
-        tex = tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum)
-        P = tracer.trace_params(wl)
-        L.check(lib.splat_trace_forward(sc.handle, C.byref(P), tex.data_ptr(), ws.data_ptr(), ws.numel(), None,
-                                        stream.cuda_stream))
-        pool.release(sid)
-        ev = torch.cuda.Event(enable_timing=True)
-        ev.record(stream)
-        pending_events.append((ev, arrive, tex))
-        if len(pending_events) > 4:
-            e, a, _ = pending_events.pop(0)
+
+    def fifo_loop():
+        ev0 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        torch.cuda.synchronize()
+        h0 = time.perf_counter()
+        plain_done = []
+        pending_events = []
+        for t, sid, wl in reqs:
+            arrive = t + 0.5
+            while time.perf_counter() - h0 < arrive:  # a request is served only once it has arrived
+                time.sleep(0.0002)
+            sc = pool.acquire(sid, 0)
+            tex = tracer.new_light_map(wl.map_w, wl.map_h, wl.n_planes, wl.accum)
+            P = tracer.trace_params(wl)
+            L.check(lib.splat_trace_forward(sc.handle, C.byref(P), tex.data_ptr(), ws.data_ptr(), ws.numel(), None,
+                                            stream.cuda_stream))
+            pool.release(sid)
+            ev = torch.cuda.Event(enable_timing=True)
+            ev.record(stream)
+            pending_events.append((ev, arrive, tex))
+            if len(pending_events) > 4:
+                e, a, _ = pending_events.pop(0)
+                e.synchronize()
+                plain_done.append((ev0.elapsed_time(e) / 1e3, a))
+        for e, a, _ in pending_events:
             e.synchronize()
             plain_done.append((ev0.elapsed_time(e) / 1e3, a))
-    for e, a, _ in pending_events:
-        e.synchronize()
-        plain_done.append((ev0.elapsed_time(e) / 1e3, a))
-    pl = np.array([d - a for d, a in plain_done])
-    plain = summarize(pl, 0.5 + arrivals[0], max(d for d, _ in plain_done), len(pl))
+        pl = np.array([d - a for d, a in plain_done])
+        return summarize(pl, 0.5 + arrivals[0], max(d for d, _ in plain_done), len(pl))
+
+    plain = fifo_loop()
+    tuned_now = {**A.get_knobs(), **A.get_knobs({L.TUNE_BATCH_PERSISTENT: (0,)})}
+    A.set_knobs(default_knobs)
+    plain_default = fifo_loop()
+    A.set_knobs(tuned_now)
 
     # capacity: the same requests all queued at once, device time to finish them
     sub = reqs[: min(len(reqs), 400)]
@@ -1090,6 +1114,9 @@ def served_result(rate: float, duration: float) -> dict:
                       "hbm_budget_gb": 150, "scene_loads": pool.loads, "scene_evictions": pool.evictions,
                       "server": "2 lanes, 128 request slots, 2^24 rays in flight"},
            "served": served, "plain_per_frame_loop": plain,
+           "plain_per_frame_loop_default_knobs": plain_default,
+           "knobs": {"tuned_on": "a captured pass of the stream's first 48 requests", **served_knobs,
+                     "tuning_trials": tuned.get("trials")},
            "capacity_frames_per_s": {"served": cap_served, "plain_per_frame_loop": cap_plain,
                                      "dropin_per_frame_loop": cap_dropin,
                                      "requests": len(sub), "note": "all requests queued at t=0; the drop-in loop is "
