@@ -851,6 +851,13 @@ static splat_status_t trace_part(const splat_scene_t* scene, const splat_trace_p
     for (int32_t b = 1; b <= P->depth; ++b) {
         RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0,
                    reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b]), packet_for(b)};
+        {
+            // the first bounce's rays are the light grid's columns in order
+            // (the range starts on a column): packet warps take 8 x 4 tiles
+            // of it instead of 32 x 1 strips (Menger step 8.20 -> 8.02 ms)
+            const int64_t gh = P->light.res1 / P->upscale;
+            if (b == 1 && gh % 8 == 0 && rb % gh == 0) src.tile_h = (int32_t)gh;
+        }
         if (b >= 2 && order_bits > 0 && P->hitter == SPLAT_HITTER_BVH && scene->d_nodes4 && scene->d_bvh_pos) {
             // secondary rays in coherent order: (octant, position of the triangle they leave)
             ProfScope ps(SPLAT_KERNEL_AUX, st);

@@ -29,6 +29,8 @@ struct RaySrc {
     int32_t packet;            // four-wide BVH: packet_form of the launch (0 one ray per lane)
     const int32_t* perm;       // BVH hitters: the k-th ray traced is ray perm[k] (nullptr: ray k); results
                                // go to the ray's own index
+    int32_t tile_h;            // packet kernels, no perm: rays are a light grid of tile_h rows in column-major
+                               // order; warps take 8 x 4 tiles of it (0: in order)
 };
 
 // Which traversal a warp of four-wide BVH rays takes, from
