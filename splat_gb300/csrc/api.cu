@@ -2006,6 +2006,9 @@ splat_status_t splat_render_camera_after(const splat_scene_t* scene, const splat
     for (int32_t b = 1; b <= P->depth; ++b) {
         RaySrc src{cur.f, cur.ignore, cur.cap, nullptr, &w.counts[b - 1], 0,
                    reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b]), packet_for(b)};
+        // camera rays are the sub-sample grid's columns in order: first-bounce
+        // packets take 8 x 4 tiles of it
+        if (b == 1 && ch % 8 == 0) src.tile_h = (int32_t)ch;
         rc = hit_any(scene, P->hitter, src, cnt, w.hit, nullptr, w.tmp, st);
         if (rc != SPLAT_OK) return rc;
         ea.in = cur;
