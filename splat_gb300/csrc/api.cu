@@ -856,7 +856,7 @@ static splat_status_t trace_part(const splat_scene_t* scene, const splat_trace_p
             // (the range starts on a column): packet warps take 8 x 4 tiles
             // of it instead of 32 x 1 strips (Menger step 8.20 -> 8.02 ms)
             const int64_t gh = P->light.res1 / P->upscale;
-            if (b == 1 && gh % 8 == 0 && rb % gh == 0) src.tile_h = (int32_t)gh;
+            if (b == 1 && rb % gh == 0 && gh <= (int64_t)kGridTileMaxRows) src.tile_h = (int32_t)gh;
         }
         if (b >= 2 && order_bits > 0 && P->hitter == SPLAT_HITTER_BVH && scene->d_nodes4 && scene->d_bvh_pos) {
             // secondary rays in coherent order: (octant, position of the triangle they leave)
@@ -2008,7 +2008,7 @@ splat_status_t splat_render_camera_after(const splat_scene_t* scene, const splat
                    reinterpret_cast<unsigned long long*>(&w.counts[kFetchBase + b]), packet_for(b)};
         // camera rays are the sub-sample grid's columns in order: first-bounce
         // packets take 8 x 4 tiles of it
-        if (b == 1 && ch % 8 == 0) src.tile_h = (int32_t)ch;
+        if (b == 1 && ch <= (int64_t)kGridTileMaxRows) src.tile_h = (int32_t)ch;
         rc = hit_any(scene, P->hitter, src, cnt, w.hit, nullptr, w.tmp, st);
         if (rc != SPLAT_OK) return rc;
         ea.in = cur;

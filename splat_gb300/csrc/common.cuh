@@ -289,6 +289,29 @@ __host__ __device__ __forceinline__ float monotonic_f32(uint32_t i) {
 constexpr uint64_t kNoHit = 0xFF80000000000001ull;  // pack_argmin(Inf, 1)
 
 // ----------------------------------------------------------------------------
+// first-bounce tiling of a light grid
+// ----------------------------------------------------------------------------
+// A grid of h rows is generated column by column (ray j at row j % h, column
+// j / h).  grid_tile_ray(p) is the ray a traversal takes as its p-th: the
+// positions are grouped by four columns; inside a group the first
+// 8 floor(h / 8) rows come as 8 x 4 tiles of 32 consecutive positions, the
+// rows below them after, column by column; columns past the last full group
+// of four keep their order.  A warp of 32 consecutive positions then holds
+// a compact patch of the grid instead of a 32 x 1 strip.  The map is a
+// bijection of 0 .. n - 1; 32-bit arithmetic, for n < 2^32 and
+// h <= kGridTileMaxRows (callers check).
+constexpr uint32_t kGridTileMaxRows = 1u << 28;
+
+__host__ __device__ __forceinline__ uint32_t grid_tile_ray(uint32_t p, uint32_t h, uint32_t n) {
+    const uint32_t span = 4u * h, g = p / span;
+    if (g >= n / span) return p;
+    const uint32_t h8 = h & ~7u, off = p - g * span;
+    if (off < 4u * h8) return (g * 4u + ((off & 31u) >> 3)) * h + (off >> 5) * 8u + (off & 7u);
+    const uint32_t o2 = off - 4u * h8, rem = h - h8;
+    return (g * 4u + o2 / rem) * h + h8 + o2 % rem;
+}
+
+// ----------------------------------------------------------------------------
 // Philox4x32-10 (Salmon et al., SC'11) and the draws of the trace step
 // ----------------------------------------------------------------------------
 __host__ __device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1) {

@@ -678,18 +678,8 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_packet_kernel(RaySrc src
         const bool valid = base + lane < n;
         const int64_t kk = valid ? base + lane : base;
         int64_t k = src.perm ? (int64_t)src.perm[kk] : kk;
-        if (!src.perm && src.tile_h > 0) {
-            // 8 x 4 tiles of the column-major grid; the tail past the last
-            // full group of four columns stays in order
-            const int64_t h = src.tile_h;
-            const int64_t region = (n / (4 * h)) * (4 * h);
-            if (kk < region) {
-                const int64_t t = kk >> 5, th = h >> 3;
-                const int64_t tc = t / th, tr = t - tc * th;
-                const int l = (int)(kk & 31);
-                k = (tc * 4 + (l >> 3)) * h + tr * 8 + (l & 7);
-            }
-        }
+        if (!src.perm && src.tile_h > 0 && n < (int64_t(1) << 32))  // 8 x 4 tiles of the grid
+            k = (int64_t)grid_tile_ray((uint32_t)kk, (uint32_t)src.tile_h, (uint32_t)n);
         const HitRay r = load_hit_ray<AOS>(src, k);
         float best;
         int32_t bi;
