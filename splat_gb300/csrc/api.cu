@@ -874,6 +874,7 @@ static splat_status_t trace_part(const splat_scene_t* scene, const splat_trace_p
         ea.hit_idx = w.hit;
         ea.bounce = (uint32_t)b;
         ea.last = b == P->depth ? 1 : 0;
+        ea.tile_h = src.tile_h;  // the first bounce's survivors leave in tile order
         {
             ProfScope ps(SPLAT_KERNEL_EVOLVE, st);
             SPLAT_CUDA(launch_evolve_trace(ea, cnt, sm, st), "evolve");
@@ -2018,6 +2019,7 @@ splat_status_t splat_render_camera_after(const splat_scene_t* scene, const splat
         ea.hit_idx = w.hit;
         ea.bounce = (uint32_t)b;
         ea.last = b == P->depth ? 1 : 0;
+        ea.tile_h = src.tile_h;
         {
             ProfScope ps(SPLAT_KERNEL_EVOLVE, st);
             SPLAT_CUDA(launch_evolve_camera(ea, cnt, sm, st), "evolve");

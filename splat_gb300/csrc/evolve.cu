@@ -166,12 +166,14 @@ __global__ void __launch_bounds__(kEvolveThreads) evolve_kernel(EvolveArgs A) {
         unsigned long long& s_base = s_base2[par];
         unsigned long long& s_dbase = s_dbase2[par];
         unsigned long long& s_sbase = s_sbase2[par];
-        const int64_t k = base + threadIdx.x;
+        int64_t k = base + threadIdx.x;
         bool keep = false, dif = false, sky = false;
         RayState r, o;
         uint32_t id = 0;
         int32_t ih = 1;
         if (k < n) {
+            if (A.tile_h > 0 && n < (int64_t(1) << 32))
+                k = (int64_t)grid_tile_ray((uint32_t)k, (uint32_t)A.tile_h, (uint32_t)n);
             r = load_ray(A.in, k);
             id = A.in.id[k];
             EvolveView v{A.tris, A.n_tris, A.err, A.first_diffuse, A.material, A.seed, A.bounce,

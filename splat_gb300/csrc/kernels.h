@@ -198,6 +198,8 @@ struct EvolveArgs {
     int64_t* splat_count;
     RaySoA sky_q;           // camera mode: rays that escaped, unchanged
     int64_t* sky_count;
+    int32_t tile_h;         // > 0: the input is a light grid of tile_h rows in column order, taken in its
+                            // 8 x 4 tiles (grid_tile_ray), so the survivors leave in tile order
 };
 cudaError_t launch_evolve_trace(const EvolveArgs& a, int64_t cap, int sm_count, cudaStream_t s);
 // trace mode plus the escaped rays queued for the skydome (camera pass)
