@@ -293,22 +293,27 @@ constexpr uint64_t kNoHit = 0xFF80000000000001ull;  // pack_argmin(Inf, 1)
 // ----------------------------------------------------------------------------
 // A grid of h rows is generated column by column (ray j at row j % h, column
 // j / h).  grid_tile_ray(p) is the ray a traversal takes as its p-th: the
-// positions are grouped by four columns; inside a group the first
-// 8 floor(h / 8) rows come as 8 x 4 tiles of 32 consecutive positions, the
-// rows below them after, column by column; columns past the last full group
-// of four keep their order.  A warp of 32 consecutive positions then holds
-// a compact patch of the grid instead of a 32 x 1 strip.  The map is a
-// bijection of 0 .. n - 1; 32-bit arithmetic, for n < 2^32 and
-// h <= kGridTileMaxRows (callers check).
-constexpr uint32_t kGridTileMaxRows = 1u << 28;
+// positions are grouped by kGridTileCols columns; inside a group the first
+// 8 floor(h / 8) rows come as 8 x 4 tiles of 32 consecutive positions, four
+// tiles side by side per tile row (so 256 consecutive positions are a
+// 16 x 16 patch), and the rows below them after, column by column; columns
+// past the last full group keep their order.  A warp of 32 consecutive
+// positions then holds a compact patch of the grid instead of a 32 x 1
+// strip.  The map is a bijection of 0 .. n - 1; 32-bit arithmetic, for
+// n < 2^32 and h <= kGridTileMaxRows (callers check).
+constexpr uint32_t kGridTileMaxRows = 1u << 26;
+constexpr uint32_t kGridTileCols = 16;  // columns per group: 4 tiles side by side
 
 __host__ __device__ __forceinline__ uint32_t grid_tile_ray(uint32_t p, uint32_t h, uint32_t n) {
-    const uint32_t span = 4u * h, g = p / span;
+    const uint32_t span = kGridTileCols * h, g = p / span;
     if (g >= n / span) return p;
     const uint32_t h8 = h & ~7u, off = p - g * span;
-    if (off < 4u * h8) return (g * 4u + ((off & 31u) >> 3)) * h + (off >> 5) * 8u + (off & 7u);
-    const uint32_t o2 = off - 4u * h8, rem = h - h8;
-    return (g * 4u + o2 / rem) * h + h8 + o2 % rem;
+    if (off < kGridTileCols * h8) {
+        const uint32_t t = off >> 5, tr = t / (kGridTileCols / 4u), tc = t - tr * (kGridTileCols / 4u);
+        return (g * kGridTileCols + tc * 4u + ((off & 31u) >> 3)) * h + tr * 8u + (off & 7u);
+    }
+    const uint32_t o2 = off - kGridTileCols * h8, rem = h - h8;
+    return (g * kGridTileCols + o2 / rem) * h + h8 + o2 % rem;
 }
 
 // ----------------------------------------------------------------------------

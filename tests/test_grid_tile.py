@@ -28,7 +28,7 @@ int main() {
             seen[k] = 1;
         }
         // a full 8 x 4 tile: the first 32 positions of a grid of >= 8 rows
-        if (h >= 8 && n >= 4 * h) {
+        if (h >= 8 && n >= kGridTileCols * h) {
             for (unsigned p = 0; p < 32; ++p) {
                 const unsigned k = grid_tile_ray(p, h, n);
                 if (k % h != p % 8 || k / h != p / 8) { std::printf("TILE n=%u h=%u p=%u\n", n, h, p); return 1; }
