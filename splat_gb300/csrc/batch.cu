@@ -61,7 +61,8 @@ struct BatchItem {
     const int32_t* bvh_pos;  // ray order: BVH position of each reference index
     int64_t key_base;        // ray order: the item's first bucket position
     int32_t pos_shift;       // ray order: low position bits dropped
-    int32_t _pad1;
+    int32_t grid_rows;       // first tick: rows of the item's light grid when its rays start on a column
+                             // (its fresh rays are taken in 8 x 4 tiles), else 0
 };
 
 struct FreshList {
@@ -128,6 +129,28 @@ __global__ void __launch_bounds__(kMaxBatchItems) batch_reserve_kernel(const Bat
     reserve_phase(items, n_slots, tick, cur_count, fresh);
 }
 
+// The pool position a kernel of this tick takes as its kk-th: fresh rays of
+// an item on its first tick in 8 x 4 tiles of the item's light grid
+// (grid_tile_ray: a bijection of the item's range), so that a warp's
+// first-bounce rays are a compact patch and evolve's survivors leave as
+// such; every other position as it is.  Hit and evolve use the same map.
+__device__ __forceinline__ int64_t fresh_tiled(const FreshList* __restrict__ fresh,
+                                               const BatchItem* __restrict__ items, int64_t kk) {
+    const int nf = fresh->n;
+    if (nf == 0 || kk < fresh->offset[0]) return kk;
+    int lo = 0, hi = nf - 1;
+    while (lo < hi) {  // last f with offset[f] <= kk
+        const int mid = (lo + hi + 1) >> 1;
+        if (fresh->offset[mid] <= kk) lo = mid;
+        else hi = mid - 1;
+    }
+    const int64_t local = kk - fresh->offset[lo];
+    const int64_t nr = fresh->prefix[lo + 1] - fresh->prefix[lo];
+    const int32_t h = items[fresh->slot[lo]].grid_rows;
+    if (h <= 0 || local >= nr) return kk;
+    return fresh->offset[lo] + (int64_t)grid_tile_ray((uint32_t)local, (uint32_t)h, (uint32_t)nr);
+}
+
 __device__ __forceinline__ void generate_phase(const BatchItem* __restrict__ items,
                                                const FreshList* __restrict__ fresh, RaySoA out, int64_t bid,
                                                int64_t nblk) {
@@ -162,7 +185,8 @@ template <bool ANY_BRUTE>
 __device__ __forceinline__ void hit_phase(RaySoA in, const int64_t* __restrict__ count,
                                           const BatchItem* __restrict__ items, int32_t* hit_idx, int32_t* err,
                                           unsigned long long* fetch, int tick, int packet_mode, int2* pstack,
-                                          const int32_t* __restrict__ perm = nullptr) {
+                                          const int32_t* __restrict__ perm = nullptr,
+                                          const FreshList* __restrict__ fresh = nullptr) {
     const int64_t n = *count;
     const int lane = threadIdx.x & 31;
     int2 stack[kBvhStack];
@@ -180,6 +204,8 @@ __device__ __forceinline__ void hit_phase(RaySoA in, const int64_t* __restrict__
                 atomicOr(err, 4);
                 k = kk;
             }
+        } else if (fresh) {
+            k = fresh_tiled(fresh, items, kk);
         }
         const HitRay r = load_hit_ray<false>(src, k);
         const uint32_t slot = in.id[k] >> kSlotShift;
@@ -215,10 +241,11 @@ __global__ void __launch_bounds__(kBatchHitThreads, 8) batch_hit_kernel(RaySoA i
                                                                         int32_t* hit_idx, int32_t* err,
                                                                         unsigned long long* fetch, int tick,
                                                                         int packet_mode,
-                                                                        const int32_t* __restrict__ perm) {
+                                                                        const int32_t* __restrict__ perm,
+                                                                        const FreshList* __restrict__ fresh) {
     __shared__ int2 s_pstack[kBatchHitThreads / 32][kPacketStack];
     hit_phase<ANY_BRUTE>(in, count, items, hit_idx, err, fetch, tick, packet_mode, s_pstack[threadIdx.x >> 5],
-                         ORDER ? perm : nullptr);
+                         ORDER ? perm : nullptr, ORDER ? nullptr : fresh);
 }
 
 // Ray-order keys of the tick's active rays and the size of every bucket
@@ -260,7 +287,7 @@ __device__ __forceinline__ void evolve_phase(RaySoA in, RaySoA out, RaySoA queue
                                              int64_t* out_count, int64_t* queue_count,
                                              const BatchItem* __restrict__ items, int tick,
                                              const int32_t* __restrict__ hit_idx, int32_t* err, int64_t bid,
-                                             int64_t nblk) {
+                                             int64_t nblk, const FreshList* __restrict__ fresh = nullptr) {
     // double-buffered by iteration parity, as in evolve_kernel
     __shared__ int s_keep2[2][kBatchThreads / 32], s_dif2[2][kBatchThreads / 32];
     __shared__ unsigned long long s_kbase2[2], s_dbase2[2];
@@ -273,11 +300,12 @@ __device__ __forceinline__ void evolve_phase(RaySoA in, RaySoA out, RaySoA queue
         int* s_dif = s_dif2[par];
         unsigned long long& s_kbase = s_kbase2[par];
         unsigned long long& s_dbase = s_dbase2[par];
-        const int64_t k = base + threadIdx.x;
+        int64_t k = base + threadIdx.x;
         bool keep = false, dif = false;
         RayState o;
         uint32_t id = 0;
         if (k < n) {
+            if (fresh) k = fresh_tiled(fresh, items, k);
             const RayState r = load_ray(in, k);
             id = in.id[k];
             const BatchItem& it = items[id >> kSlotShift];
@@ -323,9 +351,10 @@ __global__ void __launch_bounds__(kBatchThreads) batch_evolve_kernel(RaySoA in, 
                                                                      int64_t* out_count, int64_t* queue_count,
                                                                      const BatchItem* __restrict__ items, int tick,
                                                                      const int32_t* __restrict__ hit_idx,
-                                                                     int32_t* err) {
+                                                                     int32_t* err,
+                                                                     const FreshList* __restrict__ fresh) {
     evolve_phase<MK>(in, out, queue, in_count, out_count, queue_count, items, tick, hit_idx, err, blockIdx.x,
-                     gridDim.x);
+                     gridDim.x, fresh);
 }
 
 // One lane per queued ray, walking all of its planes: rays of one item are
@@ -536,7 +565,7 @@ cudaError_t launch_batch_trace(const BatchTickArgs& a, cudaStream_t s) {
             const int grid = resident_grid(reinterpret_cast<const void*>(kernel), a.cap_rays, a.sm_count,
                                            kBatchHitThreads, g_tune[SPLAT_TUNE_BVH_BLOCKS_PER_SM]);
             kernel<<<grid, kBatchHitThreads, 0, s>>>(a.cur, a.cur_count, items, a.hit_idx, a.err, a.fetch, a.tick,
-                                                      mode, perm);
+                                                      mode, perm, fresh);
         };
         if (a.any_brute)
             perm ? hit(batch_hit_kernel<true, true>) : hit(batch_hit_kernel<true, false>);
@@ -546,7 +575,7 @@ cudaError_t launch_batch_trace(const BatchTickArgs& a, cudaStream_t s) {
         const int eg = grid_cap(a.cap_rays, kBatchThreads, a.sm_count, g_tune[SPLAT_TUNE_EVOLVE_BLOCKS_PER_SM]);
 #define SPLAT_BATCH_EVOLVE(MK)                                                                            \
     batch_evolve_kernel<MK><<<eg, kBatchThreads, 0, s>>>(a.cur, a.next, a.queue, a.cur_count, a.next_count, \
-                                                         a.queue_count, items, a.tick, a.hit_idx, a.err)
+                                                         a.queue_count, items, a.tick, a.hit_idx, a.err, fresh)
         switch (a.material_kind) {
             case SPLAT_MATERIAL_LINEAR_REF: SPLAT_BATCH_EVOLVE(SPLAT_MATERIAL_LINEAR_REF); break;
             case SPLAT_MATERIAL_CAUCHY: SPLAT_BATCH_EVOLVE(SPLAT_MATERIAL_CAUCHY); break;
@@ -597,6 +626,8 @@ void batch_fill_item(void* dst, const BatchSceneRef& sc, const GenParams& gen, i
     it.material = material;
     it.sp = sp;
     it.bvh_pos = sc.nodes4 ? sc.bvh_pos : nullptr;
+    const int64_t rows = gen.light.res1 / gen.upscale;
+    it.grid_rows = (rows >= 1 && rows <= (int64_t)kGridTileMaxRows && gen.ray_begin % rows == 0) ? (int32_t)rows : 0;
     std::memcpy(dst, &it, sizeof(it));
 }
 
