@@ -311,6 +311,33 @@ def test_ray_ranges_on_concurrent_streams(torch_cuda, accum):
     assert one.sum() > 0
 
 
+@pytest.mark.parametrize("res1,res2", [(37, 53), (24, 100), (9, 70), (5, 33)])
+def test_tiled_first_bounce_on_odd_grids(torch_cuda, res1, res2):
+    """The first bounce's packets and evolve take a light grid in 8 x 4
+    tiles of groups of 16 columns; rows past the last multiple of 8, and
+    columns past the last full group, follow in order.  On grids of every
+    such shape, with packets on every bounce and whole or column-straddling
+    ray ranges, the int32 map and the per-bounce counts equal the oracle's."""
+    from splat_gb300 import _lib as L
+
+    lib = L.load()
+    base = S.plain_small()
+    light = base.light.copy()
+    light["res1"], light["res2"] = res1, res2
+    wl = S.plain_small(light=light, accum="i32", hitter="bvh")
+    old = lib.splat_get_tuning(L.TUNE_BVH_PACKET)
+    try:
+        L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, 2))
+        n = res1 * res2
+        for rb, re in ((0, 0), (res1 + 3, n - 5), (2 * res1, n)):
+            got, st = _gpu(wl, ray_begin=rb, ray_end=re)
+            ref_tex, ref_st, _ = O.trace_forward(wl, ray_begin=rb, ray_end=re if re else n)
+            assert st["rays_per_bounce"] == [int(x) for x in ref_st[: wl.depth]], (rb, re)
+            _cmp(wl, got, ref_tex)
+    finally:
+        L.check(lib.splat_set_tuning(L.TUNE_BVH_PACKET, old))
+
+
 def test_counted_traversal_work_matches_the_frame(torch_cuda):
     """The counting kernels (SPLAT_TUNE_COUNT_WORK) trace the same rays as
     the plain ones -- same map, same statistics -- and count every traced
