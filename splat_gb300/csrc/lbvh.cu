@@ -642,7 +642,11 @@ cudaError_t launch_ray_order(const float* soa_f, const int32_t* ignore, int64_t 
                                                         n_pos, keys, cnt);
     ++g_launches;
     if ((e = scan_u32(cnt, buckets, sums, s)) != cudaSuccess) return e;
-    ray_bucket_place_kernel<<<(unsigned)b, 256, 0, s>>>(keys, cap, d_count, cnt, perm);
+    // one block per 256 rays (blocks start in index order), so a bucket's
+    // slots go to its rays nearly in position order: the input order carries
+    // the first bounce's tiles
+    const int64_t bp = (cap + 255) / 256;
+    ray_bucket_place_kernel<<<(unsigned)(bp < 1 ? 1 : bp), 256, 0, s>>>(keys, cap, d_count, cnt, perm);
     ++g_launches;
     *perm_out = perm;
     return cudaGetLastError();
@@ -655,9 +659,9 @@ cudaError_t launch_order_place(const uint32_t* keys, int64_t cap, const int64_t*
     if (cap < 1 || buckets < 1) return cudaSuccess;
     cudaError_t e = scan_u32(cnt, buckets, sums, s);
     if (e != cudaSuccess) return e;
-    int64_t b = (cap + 255) / 256;
-    if (b > (int64_t)sm_count * 8) b = (int64_t)sm_count * 8;
+    int64_t b = (cap + 255) / 256;  // one block per 256 rays, as in launch_ray_order
     if (b < 1) b = 1;
+    (void)sm_count;
     ray_bucket_place_kernel<<<(unsigned)b, 256, 0, s>>>(keys, cap, d_count, cnt, perm);
     ++g_launches;
     return cudaGetLastError();
