@@ -130,8 +130,8 @@ __global__ void radix_hist_kernel(const uint32_t* __restrict__ keys, int64_t n, 
 }
 
 // Stable scatter: a key's rank among the tile's keys with its digit is the
-// count in earlier rounds, in earlier warps of this round, and in earlier
-// lanes of its warp (__match_any_sync peers).
+// count in the tile's earlier passes of the block, in earlier warps of this
+// pass, and in earlier lanes of its warp (__match_any_sync peers).
 __global__ void radix_scatter_kernel(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals, int64_t n,
                                      int shift, const uint32_t* __restrict__ hist, int64_t tiles, uint32_t* keys_out,
                                      uint32_t* vals_out, const int64_t* d_n) {
