@@ -233,8 +233,11 @@ __device__ __forceinline__ void hit_phase(RaySoA in, const int64_t* __restrict__
 
 constexpr int kBatchHitThreads = 128;
 
-// ORDER: the rays are read through the ray-order permutation perm (the
-// plain form, without it, keeps its register count and occupancy).
+// ORDER: the rays are read through the ray-order permutation perm (where an
+// item's fresh rays sit in one bucket per octant, in placement order);
+// otherwise in pool order with each item's first-tick rays in 8 x 4 tiles of
+// its light grid (fresh_tiled).  Separate instantiations, so the form
+// without perm keeps its register count.
 template <bool ANY_BRUTE, bool ORDER>
 __global__ void __launch_bounds__(kBatchHitThreads, 8) batch_hit_kernel(RaySoA in, const int64_t* __restrict__ count,
                                                                         const BatchItem* __restrict__ items,
