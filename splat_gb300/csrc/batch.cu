@@ -281,6 +281,32 @@ __global__ void batch_order_count_kernel(RaySoA in, const int64_t* __restrict__ 
     }
 }
 
+// Slots of the ray order: every ray takes the next slot of its bucket, one
+// atomic per group of equal keys in a warp.  Threads take the pool in the
+// order the unordered hit kernel would (an item's fresh rays in tiles), and
+// one block per 256 rays starts in index order, so a bucket's rays keep
+// nearly that order.
+__global__ void batch_order_place_kernel(const uint32_t* __restrict__ keys, const int64_t* __restrict__ count,
+                                         int64_t cap_rays, int64_t pool_cap, uint32_t* __restrict__ off,
+                                         int32_t* __restrict__ perm, const BatchItem* __restrict__ items,
+                                         const FreshList* __restrict__ fresh) {
+    const int64_t n = min(min(pool_cap, cap_rays), *count);
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x + threadIdx.x - lane; base < n; base += stride) {
+        const bool valid = base + lane < n;
+        const int64_t k = valid ? fresh_tiled(fresh, items, base + lane) : 0;
+        const uint32_t key = valid ? keys[k] : 0xffffffffu;
+        const unsigned peers = __match_any_sync(0xffffffffu, key);
+        const int leader = __ffs(peers) - 1;
+        uint32_t slot = 0;
+        if (valid && lane == leader) slot = atomicAdd(&off[key], (uint32_t)__popc(peers));
+        slot = __shfl_sync(0xffffffffu, slot, leader);
+        if (valid) perm[slot + (uint32_t)__popc(peers & below)] = (int32_t)k;
+    }
+}
+
 constexpr int kBatchThreads = 256;
 
 // MK >= 0: every item in flight has this material kind (compile-time, so
@@ -559,9 +585,10 @@ cudaError_t launch_batch_trace(const BatchTickArgs& a, cudaStream_t s) {
             batch_order_count_kernel<<<grid_cap(a.cap_rays, 256, a.sm_count, 8), 256, 0, s>>>(
                 a.cur, a.cur_count, a.cap_rays, items, a.order_keys, a.order_cnt);
             ++g_launches;
-            e = launch_order_place(a.order_keys, a.cap_rays, a.cur_count, a.order_cnt, a.order_buckets, a.order_sums,
-                                   a.order_perm, a.sm_count, s);
-            if (e != cudaSuccess) return e;
+            if ((e = launch_order_scan(a.order_cnt, a.order_buckets, a.order_sums, s)) != cudaSuccess) return e;
+            batch_order_place_kernel<<<(unsigned)((a.cap_rays + 255) / 256), 256, 0, s>>>(
+                a.order_keys, a.cur_count, a.cap_rays, a.cur.cap, a.order_cnt, a.order_perm, items, fresh);
+            ++g_launches;
             perm = a.order_perm;
         }
         auto hit = [&](auto kernel) {

@@ -131,14 +131,11 @@ cudaError_t launch_ray_order(const float* soa_f, const int32_t* ignore, int64_t 
                              const int32_t* bvh_pos, int64_t n_tris, int key_bits, void* scratch,
                              const int32_t** perm_out, int sm_count, cudaStream_t s);
 
-// The placement half of that counting sort for keys computed elsewhere: cnt
-// holds each bucket's size (buckets entries), is scanned in place into
-// offsets (sums: order_sums_count(buckets) words of scratch), and every one
-// of the d_count rays takes a slot of its bucket in perm (one atomic per
-// group of equal keys in a warp).
+// The bucket offsets of that counting sort for keys counted elsewhere: cnt
+// holds each bucket's size (buckets entries) and is scanned in place into
+// offsets (sums: order_sums_count(buckets) words of scratch).
 size_t order_sums_count(int64_t buckets);
-cudaError_t launch_order_place(const uint32_t* keys, int64_t cap, const int64_t* d_count, uint32_t* cnt,
-                               int64_t buckets, uint32_t* sums, int32_t* perm, int sm_count, cudaStream_t s);
+cudaError_t launch_order_scan(uint32_t* cnt, int64_t buckets, uint32_t* sums, cudaStream_t s);
 
 // scene packing / refit.  scale: device word holding max |vertex coordinate|
 // (float bits), from which every padded box takes pad_abs = 1e-4 max(1, scale).

@@ -654,17 +654,9 @@ cudaError_t launch_ray_order(const float* soa_f, const int32_t* ignore, int64_t 
 
 size_t order_sums_count(int64_t buckets) { return (size_t)n_tiles_of(buckets < 1 ? 1 : buckets); }
 
-cudaError_t launch_order_place(const uint32_t* keys, int64_t cap, const int64_t* d_count, uint32_t* cnt,
-                               int64_t buckets, uint32_t* sums, int32_t* perm, int sm_count, cudaStream_t s) {
-    if (cap < 1 || buckets < 1) return cudaSuccess;
-    cudaError_t e = scan_u32(cnt, buckets, sums, s);
-    if (e != cudaSuccess) return e;
-    int64_t b = (cap + 255) / 256;  // one block per 256 rays, as in launch_ray_order
-    if (b < 1) b = 1;
-    (void)sm_count;
-    ray_bucket_place_kernel<<<(unsigned)b, 256, 0, s>>>(keys, cap, d_count, cnt, perm);
-    ++g_launches;
-    return cudaGetLastError();
+cudaError_t launch_order_scan(uint32_t* cnt, int64_t buckets, uint32_t* sums, cudaStream_t s) {
+    if (buckets < 1) return cudaSuccess;
+    return scan_u32(cnt, buckets, sums, s);
 }
 
 }  // namespace splat
