@@ -660,7 +660,10 @@ __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_refill_kernel(RaySrc src
 // Packet form: each warp traverses its 32 rays together (bvh4_closest_packet)
 // on a shared-memory stack.  ADAPT: per warp, packets only when its rays are
 // coherent by packet_coherent's thresholds of `form` (2 loose, 3 tight);
-// otherwise one ray per lane.
+// otherwise one ray per lane.  Rays are taken through src.perm when set, or,
+// with src.tile_h set (a first bounce: the light grid's columns in order),
+// in 8 x 4 tiles of the grid (grid_tile_ray), so a warp holds a compact
+// patch of rays.
 template <bool AOS, bool ADAPT, bool COUNT = false>
 __global__ void __launch_bounds__(kBvhThreads) hit_bvh4_packet_kernel(RaySrc src, Bvh4View bvh,
                                                                       int32_t* __restrict__ hit_idx,
